@@ -1,0 +1,442 @@
+"""GB300-native dilation-based Hausdorff distance for 3D binary masks.
+
+Python mirror of the C ABI in include/hd/hd.h (libhd_gb300.so, hand-written
+sm_103a kernels).  The reference's entry point is the C++ call
+``HausdorffDistance::computeDistance(Volume*, Volume*)``
+(forBench/HausdorffDistance.cuh:17); :class:`HausdorffDistance` and
+:class:`Volume` below mirror it, and :class:`Context` exposes the rest
+(device-resident inputs, batches, profiling, distance maps, autotuning) and
+:class:`Server` the continuous-batching request loop.
+
+Masks are ``(D, H, W)`` arrays (x fastest, like ``Volume``), numpy arrays or
+torch tensors on the CPU or on the GPU; nonzero is foreground.  Metric names:
+``"se6"`` (6-neighbour element, Manhattan distance) and ``"se18"`` (the
+reference's default 18-neighbour element, forBench/HausdorffDistance.cu:35-58).
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from . import _native as N
+from ._native import (HD_EMPTY_MASK, HD_ERR_BAD_ARG, HD_ERR_BUSY, HD_ERR_CANCELLED, HD_ERR_CUDA,
+                      HD_ERR_ITER_LIMIT, HD_ERR_NOT_READY, HD_ERR_OOM, HD_ERR_TIMEOUT,
+                      HD_ERR_UNSUPPORTED, HD_OK, HD_SE6, HD_SE18_FORBENCH)
+
+__all__ = [
+    "Context", "Server", "HausdorffDistance", "Volume", "HDError", "metric_code", "load_hdf5_bool",
+    "HD_OK", "HD_EMPTY_MASK", "HD_ERR_BAD_ARG", "HD_ERR_OOM", "HD_ERR_CUDA", "HD_ERR_TIMEOUT",
+    "HD_ERR_CANCELLED", "HD_ERR_ITER_LIMIT", "HD_ERR_NOT_READY", "HD_ERR_UNSUPPORTED", "HD_ERR_BUSY",
+    "HD_SE6", "HD_SE18_FORBENCH",
+]
+
+_METRICS = {"se6": HD_SE6, "se18": HD_SE18_FORBENCH, HD_SE6: HD_SE6, HD_SE18_FORBENCH: HD_SE18_FORBENCH}
+
+
+class HDError(RuntimeError):
+    """A library call returned a hard error (anything but OK / EMPTY_MASK)."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{N.status_string(code)} ({code}): {message}")
+        self.code = code
+
+
+def metric_code(metric) -> int:
+    try:
+        return _METRICS[metric]
+    except KeyError:
+        raise ValueError(f"unknown metric {metric!r}; use 'se6' or 'se18'") from None
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def _dims(x):
+    if len(x.shape) != 3:
+        raise ValueError("masks must have shape (D, H, W)")
+    D, H, W = (int(v) for v in x.shape)
+    return W, H, D
+
+
+class _Buf:
+    """Pointer to a contiguous uint8 view of a mask (keeps the owner alive)."""
+
+    def __init__(self, x):
+        if _is_torch(x):
+            import torch
+            t = x
+            if t.dtype != torch.uint8:
+                t = (t != 0).to(torch.uint8)
+            t = t.contiguous()
+            self.obj = t
+            self.ptr = t.data_ptr()
+            self.on_device = t.is_cuda
+        else:
+            a = np.ascontiguousarray(x)
+            if a.dtype != np.uint8:
+                a = (a != 0).astype(np.uint8)
+            self.obj = a
+            self.ptr = a.ctypes.data
+            self.on_device = False
+        self.W, self.H, self.D = _dims(self.obj)
+
+
+def _check(code: int, ctx_handle, allow_empty=True):
+    if code == HD_OK or (allow_empty and code == HD_EMPTY_MASK):
+        return
+    msg = ""
+    if ctx_handle:
+        msg = (N.load().hd_context_last_error(ctx_handle) or b"").decode()
+    raise HDError(code, msg)
+
+
+def _current_stream_ptr():
+    import torch
+    return torch.cuda.current_stream().cuda_stream
+
+
+class Context:
+    """A device context of the library (hd_context_create).
+
+    Options mirror ``hd_options``: brick_x_words / brick_z (brick shape; 0 =
+    tuned), ctas_per_sm (0 = occupancy maximum), max_iterations (0 = W+H+D),
+    barrier_timeout_ns (0 = 10 s), percentile (robust HD, default 0.95),
+    zero_copy (host masks read in place when the device can), tuning_table
+    (JSON path of the autotuner's table).
+    """
+
+    def __init__(self, device: int = 0, *, brick_x_words=0, brick_z=0, ctas_per_sm=0, max_iterations=0,
+                 barrier_timeout_ns=0, percentile=0.95, zero_copy=True, tuning_table=None):
+        L = N.load()
+        opt = N.HdOptions()
+        L.hd_options_init(ctypes.byref(opt))
+        opt.brick_x_words = brick_x_words
+        opt.brick_z = brick_z
+        opt.ctas_per_sm = ctas_per_sm
+        opt.max_iterations = max_iterations
+        opt.barrier_timeout_ns = barrier_timeout_ns
+        opt.percentile = percentile
+        opt.zero_copy = 1 if zero_copy else 0
+        self._tuning = tuning_table.encode() if tuning_table else None
+        opt.tuning_table = self._tuning
+        h = ctypes.c_void_p()
+        code = L.hd_context_create(int(device), ctypes.byref(opt), ctypes.byref(h))
+        if code != HD_OK:
+            raise HDError(code, f"hd_context_create(device={device})")
+        self._h = h
+        self.device = device
+
+    # -- lifetime -----------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            N.load().hd_context_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def last_error(self) -> str:
+        return (N.load().hd_context_last_error(self._h) or b"").decode()
+
+    # -- single pair --------------------------------------------------------
+    def compute(self, a, b, metric="se6", stream=None) -> dict:
+        """HD of one pair.  Host inputs go through hd_compute_u8 (copies or
+        zero-copy reads inside the call); CUDA tensors through
+        hd_compute_u8_device on `stream` (default: torch's current stream)."""
+        A, B = _Buf(a), _Buf(b)
+        if (A.W, A.H, A.D) != (B.W, B.H, B.D):
+            raise ValueError("mask shapes differ")
+        if A.on_device != B.on_device:
+            raise ValueError("both masks must be on the host or both on the device")
+        r = N.HdResult()
+        L = N.load()
+        if A.on_device:
+            s = _current_stream_ptr() if stream is None else stream
+            code = L.hd_compute_u8_device(self._h, A.ptr, B.ptr, A.W, A.H, A.D, metric_code(metric),
+                                          ctypes.c_void_p(s), ctypes.byref(r))
+        else:
+            code = L.hd_compute_u8(self._h, A.ptr, B.ptr, A.W, A.H, A.D, metric_code(metric), ctypes.byref(r))
+        _check(code, self._h)
+        return r.as_dict()
+
+    def compute_device(self, a, b, metric="se6", stream=None) -> dict:
+        return self.compute(a, b, metric, stream)
+
+    # -- batches --------------------------------------------------------------
+    def batch(self, pairs: Sequence, metric="se6") -> list:
+        """One hd_batch_compute over [(a, b), ...] (host or CUDA masks)."""
+        n = len(pairs)
+        if n == 0:
+            return []
+        bufs = []
+        descs = (N.HdPairDesc * n)()
+        for i, (a, b) in enumerate(pairs):
+            A, B = _Buf(a), _Buf(b)
+            if (A.W, A.H, A.D) != (B.W, B.H, B.D) or A.on_device != B.on_device:
+                raise ValueError(f"pair {i}: shapes or devices differ")
+            bufs.append((A, B))
+            descs[i].a, descs[i].b = A.ptr, B.ptr
+            descs[i].W, descs[i].H, descs[i].D = A.W, A.H, A.D
+            descs[i].metric = metric_code(metric)
+            descs[i].on_device = 1 if A.on_device else 0
+        res = (N.HdResult * n)()
+        code = N.load().hd_batch_compute(self._h, descs, n, res)
+        _check(code, self._h)
+        return [res[i].as_dict() for i in range(n)]
+
+    # -- instrumentation --------------------------------------------------------
+    def profile(self, a, b, metric="se6"):
+        """Instrumented run (CUDA masks): result, per-step 32^3 tile counts of
+        both directions (tiles_ab: dilation of B covering A) and bricks
+        processed."""
+        A, B = _Buf(a), _Buf(b)
+        if not (A.on_device and B.on_device):
+            raise ValueError("profile() takes CUDA tensors")
+        n = A.W + A.H + A.D + 1
+        tab = np.zeros(n, np.uint64)
+        tba = np.zeros(n, np.uint64)
+        bricks = ctypes.c_uint64(0)
+        r = N.HdResult()
+        u64p = ctypes.POINTER(ctypes.c_uint64)
+        code = N.load().hd_profile_u8_device(self._h, A.ptr, B.ptr, A.W, A.H, A.D, metric_code(metric),
+                                             ctypes.byref(r), tab.ctypes.data_as(u64p),
+                                             tba.ctypes.data_as(u64p), n, ctypes.byref(bricks))
+        _check(code, self._h)
+        return r.as_dict(), tab, tba, int(bricks.value)
+
+    def distance_map(self, a, b, metric="se6"):
+        """Per-voxel distances (CUDA masks): int32 maps, map_a[v] = d(v, B) on
+        A minus B, 0 on the overlap, -1 elsewhere (map_b likewise)."""
+        import torch
+        A, B = _Buf(a), _Buf(b)
+        if not (A.on_device and B.on_device):
+            raise ValueError("distance_map() takes CUDA tensors")
+        ma = torch.empty(A.obj.shape, dtype=torch.int32, device=A.obj.device)
+        mb = torch.empty(A.obj.shape, dtype=torch.int32, device=A.obj.device)
+        r = N.HdResult()
+        code = N.load().hd_distance_map_device(self._h, A.ptr, B.ptr, A.W, A.H, A.D, metric_code(metric),
+                                               ma.data_ptr(), mb.data_ptr(), ctypes.byref(r))
+        _check(code, self._h)
+        return r.as_dict(), ma, mb
+
+    def autotune(self, pairs: Sequence, metric="se6", repeats: int = 3) -> str:
+        n = len(pairs)
+        bufs = []
+        descs = (N.HdPairDesc * n)()
+        for i, (a, b) in enumerate(pairs):
+            A, B = _Buf(a), _Buf(b)
+            bufs.append((A, B))
+            descs[i].a, descs[i].b = A.ptr, B.ptr
+            descs[i].W, descs[i].H, descs[i].D = A.W, A.H, A.D
+            descs[i].metric = metric_code(metric)
+            descs[i].on_device = 1 if A.on_device else 0
+        rep = ctypes.create_string_buffer(8192)
+        code = N.load().hd_autotune(self._h, descs, n, int(repeats), rep, len(rep))
+        _check(code, self._h, allow_empty=False)
+        return rep.value.decode()
+
+
+class Server:
+    """Continuous-batching request loop (hd_server_*) on a Context."""
+
+    def __init__(self, ctx: Context, *, hbm_budget_bytes=0, max_inflight=0, max_queue=0, tick_iterations=0,
+                 metric="se6"):
+        L = N.load()
+        opt = N.HdServerOptions()
+        L.hd_server_options_init(ctypes.byref(opt))
+        if hbm_budget_bytes:
+            opt.hbm_budget_bytes = int(hbm_budget_bytes)
+        if max_inflight:
+            opt.max_inflight = int(max_inflight)
+        if max_queue:
+            opt.max_queue = int(max_queue)
+        if tick_iterations:
+            opt.tick_iterations = int(tick_iterations)
+        opt.metric = metric_code(metric)
+        self.metric = opt.metric
+        h = ctypes.c_void_p()
+        code = L.hd_server_create(ctx.handle, ctypes.byref(opt), ctypes.byref(h))
+        if code != HD_OK:
+            raise HDError(code, "hd_server_create")
+        self._h = h
+        self._ctx = ctx
+        self._keep = {}
+
+    def submit(self, a, b) -> int:
+        A, B = _Buf(a), _Buf(b)
+        d = N.HdPairDesc()
+        d.a, d.b = A.ptr, B.ptr
+        d.W, d.H, d.D = A.W, A.H, A.D
+        d.metric = self.metric
+        d.on_device = 1 if A.on_device else 0
+        t = ctypes.c_uint64(0)
+        code = N.load().hd_server_submit(self._h, ctypes.byref(d), ctypes.byref(t))
+        if code != HD_OK:
+            raise HDError(code, "hd_server_submit")
+        if A.on_device:
+            self._keep[int(t.value)] = (A, B)  # device masks must outlive the request
+        return int(t.value)
+
+    def poll(self, ticket: int):
+        r = N.HdResult()
+        code = N.load().hd_server_poll(self._h, ticket, ctypes.byref(r))
+        if code == HD_ERR_NOT_READY:
+            return None
+        if code != HD_OK:
+            raise HDError(code, "hd_server_poll")
+        self._keep.pop(ticket, None)
+        return r.as_dict()
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        r = N.HdResult()
+        code = N.load().hd_server_wait(self._h, ticket, int(timeout_ms), ctypes.byref(r))
+        if code == HD_ERR_NOT_READY:
+            return None
+        if code != HD_OK:
+            raise HDError(code, "hd_server_wait")
+        self._keep.pop(ticket, None)
+        return r.as_dict()
+
+    def cancel(self, ticket: int):
+        code = N.load().hd_server_cancel(self._h, ticket)
+        if code != HD_OK:
+            raise HDError(code, "hd_server_cancel")
+
+    def stats(self) -> dict:
+        s = N.HdServerStats()
+        N.load().hd_server_get_stats(self._h, ctypes.byref(s))
+        return s.as_dict()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.load().hd_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Volume:
+    """Mirror of the reference's Volume (forBench/Volume.h:7-26): a zeroed
+    byte mask with x + W*y + W*H*z indexing."""
+
+    def __init__(self, width: int, height: int, depth: int = 1):
+        self.width, self.height, self.depth = int(width), int(height), int(depth)
+        self.volume = np.zeros((self.depth, self.height, self.width), np.uint8)
+
+    @classmethod
+    def from_array(cls, arr) -> "Volume":
+        a = np.ascontiguousarray(arr)
+        v = cls(a.shape[2], a.shape[1], a.shape[0])
+        v.volume[...] = a != 0
+        return v
+
+    def getVoxelValue(self, x, y, z) -> bool:
+        return bool(self.volume[z, y, x])
+
+    def getPixelValue(self, x, y) -> bool:
+        return bool(self.volume[0, y, x])
+
+    def setVoxelValue(self, value, x, y, z):
+        self.volume[z, y, x] = 1 if value else 0
+
+    def setPixelValue(self, value, x, y):
+        self.volume[0, y, x] = 1 if value else 0
+
+    def getWidth(self):
+        return self.width
+
+    def getHeight(self):
+        return self.height
+
+    def getDepth(self):
+        return self.depth
+
+    def getVolume(self):
+        return self.volume
+
+    def dispose(self):
+        self.volume = None
+
+
+class HausdorffDistance:
+    """Mirror of the reference's class (forBench/HausdorffDistance.cuh:11-19).
+
+    computeDistance(img1, img2) returns the HD as an int like the reference
+    (forBench/HausdorffDistance.cu:185); the sizes of img1 are used for both
+    masks (:103).  Instead of exiting the process or looping forever it
+    returns -1 on error or when exactly one mask is empty.  The default element
+    is the reference's shipped one (CHEBYSHEV 1 -> "se18")."""
+
+    _ctx = None
+
+    def __init__(self, metric="se18", device: int = 0):
+        self.metric = metric_code(metric)
+        self.device = device
+
+    @classmethod
+    def _context(cls, device):
+        if cls._ctx is None:
+            cls._ctx = Context(device)
+        return cls._ctx
+
+    def computeResult(self, img1: Volume, img2: Volume) -> dict:
+        W, H, D = img1.getWidth(), img1.getHeight(), img1.getDepth()
+        b = np.ascontiguousarray(img2.getVolume()).reshape(-1)[: W * H * D].reshape(D, H, W)
+        return self._context(self.device).compute(img1.getVolume(), b, self.metric)
+
+    def computeDistance(self, img1: Volume, img2: Volume) -> int:
+        try:
+            r = self.computeResult(img1, img2)
+        except HDError:
+            return -1
+        return int(r["hd"]) if r["status"] == HD_OK else -1
+
+    def computeDistances(self, img1: Volume, img2: Volume):
+        """(max HD, average HD), (-1, -1.0) on error."""
+        try:
+            r = self.computeResult(img1, img2)
+        except HDError:
+            return -1, -1.0
+        if r["status"] != HD_OK:
+            return -1, -1.0
+        return int(r["hd"]), float(r["avg_hd"])
+
+
+def load_hdf5_bool(path: str, dataset: str) -> np.ndarray:
+    """loadHDFIntoBoolArr (forBench/hdf5Manag.cu:44-86): flat uint8 array."""
+    L = N.load()
+    p = ctypes.c_void_p()
+    n = ctypes.c_size_t(0)
+    code = L.hd_load_hdf5_bool(path.encode(), dataset.encode(), ctypes.byref(p), ctypes.byref(n))
+    if code != HD_OK:
+        raise HDError(code, f"hd_load_hdf5_bool({path!r}, {dataset!r})")
+    try:
+        return np.ctypeslib.as_array((ctypes.c_uint8 * n.value).from_address(p.value)).copy()
+    finally:
+        L.hd_free(p)

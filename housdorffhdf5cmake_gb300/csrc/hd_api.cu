@@ -1,0 +1,722 @@
+// hd_api.cu -- host orchestration behind the C ABI (include/hd/hd.h).
+//
+// Replaces HausdorffDistance::computeDistance (forBench/HausdorffDistance.cu:
+// 101-187) and the prototype's orchestration (hello.cu:892-1055, 1910-2062).
+// Per call: one upload of descriptors, the packing launch, the set-up launch,
+// ONE cooperative launch of the persistent dilation kernel that runs every
+// step on the device, and one read-back of a few hundred bytes.  No host
+// round trip per step (the reference does a blocking symbol read per step at
+// :167), no cudaDeviceReset, no exit.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "hd/hd.h"
+#include "hd_internal.h"
+#include "hd_kernels.h"
+
+using hdk::Ctl;
+using hdk::Job;
+using hdk::JobState;
+using hdk::PairDesc;
+using hdk::PairInfo;
+
+namespace hdh {
+
+namespace {
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t x, size_t a = kAlign) { return (x + a - 1) / a * a; }
+constexpr long long kMaxWords = (1LL << 31) - 1;
+}  // namespace
+
+cudaError_t DeviceArena::ensure(size_t n) {
+    if (n <= cap) return cudaSuccess;
+    release();
+    size_t want = std::max(n, cap + cap / 4);
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        ptr = nullptr;
+        e = cudaMalloc(&ptr, n);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            ptr = nullptr;
+            cap = 0;
+            return e;
+        }
+        want = n;
+    }
+    cap = want;
+    return cudaSuccess;
+}
+
+void DeviceArena::release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+}
+
+cudaError_t PinnedArena::ensure(size_t n) {
+    if (n <= cap) return cudaSuccess;
+    release();
+    const size_t want = std::max(n, (size_t)1 << 16);
+    cudaError_t e = cudaHostAlloc(&ptr, want, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        ptr = nullptr;
+        cap = 0;
+        return e;
+    }
+    cap = want;
+    return cudaSuccess;
+}
+
+void PinnedArena::release() {
+    if (ptr) cudaFreeHost(ptr);
+    ptr = nullptr;
+    cap = 0;
+}
+
+DeviceGuard::DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+        cudaGetLastError();
+        prev = -1;
+    }
+    ok = cudaSetDevice(dev) == cudaSuccess;
+    if (!ok) cudaGetLastError();
+}
+
+DeviceGuard::~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+}
+
+hd_status set_error(hd_context* ctx, hd_status st, const char* fmt, ...) {
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        ctx->last_error = buf;
+    }
+    return st;
+}
+
+hd_status cuda_fail(hd_context* ctx, cudaError_t e, const char* where) {
+    const hd_status st = (e == cudaErrorMemoryAllocation) ? HD_ERR_OOM : HD_ERR_CUDA;
+    set_error(ctx, st, "%s: %s (%s)", where, cudaGetErrorString(e), cudaGetErrorName(e));
+    cudaGetLastError();
+    return st;
+}
+
+hd_status check_dims(hd_context* ctx, int32_t W, int32_t H, int32_t D) {
+    if (W <= 0 || H <= 0 || D <= 0)
+        return set_error(ctx, HD_ERR_BAD_ARG, "sizes must be positive (W=%d H=%d D=%d)", W, H, D);
+    const long long wx = (W + 31) / 32;
+    const long long pitch = (wx + 3) / 4 * 4;
+    if (pitch * H * D > kMaxWords)
+        return set_error(ctx, HD_ERR_BAD_ARG, "volume %dx%dx%d exceeds 2^31 packed words", W, H, D);
+    if ((long long)W + H + D > (1 << 24))
+        return set_error(ctx, HD_ERR_BAD_ARG, "volume %dx%dx%d too long", W, H, D);
+    return HD_OK;
+}
+
+const uint8_t* zero_copy_ptr(hd_context* ctx, const uint8_t* p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) == cudaSuccess) {
+        if (at.type == cudaMemoryTypeHost && at.devicePointer) return (const uint8_t*)at.devicePointer;
+        if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return p;
+    } else {
+        cudaGetLastError();
+    }
+    if (ctx->pageable_ats) return p;
+    return nullptr;
+}
+
+int robust_k(const uint64_t* hist, int len, uint64_t total, float p) {
+    // hello.cu:1751-1758: continue while (float)total * robustnessPercent > covered.
+    const float tf = (float)total * p;
+    uint64_t cov = 0;
+    for (int k = 0; k < len; ++k) {
+        if (k > 0) cov += hist[k];
+        if (!(tf > (float)cov)) return k;
+    }
+    return len - 1;
+}
+
+int occupancy_of(hd_context* ctx, const void* fn) {
+    auto it = ctx->occupancy.find(fn);
+    if (it != ctx->occupancy.end()) return it->second;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, 256, 0) != cudaSuccess) {
+        cudaGetLastError();
+        n = 1;
+    }
+    n = std::max(1, n);
+    ctx->occupancy[fn] = n;
+    return n;
+}
+
+namespace {
+
+struct PairPlan {
+    int wxf;
+    long long full_words;   // packed full volume, one mask
+    long long dom_words;    // domain capacity (pitch_full * H * D), one buffer
+    long long bricks;       // per job, upper bound
+    int kmax;
+    long long tiles;        // full-volume 32^3 tiles (instrumented runs)
+    size_t off_pa, off_pb, off_jb[2][3], off_in_a, off_in_b, off_hist, off_tstamp[2], off_tcount[2];
+    unsigned long long brick0;
+};
+
+}  // namespace
+
+hd_status decode_result(const hdk::PairInfo& I, const hdk::JobState& s0, const hdk::JobState& s1,
+                        const uint64_t* hist_ab, const uint64_t* hist_ba, int kp1, int iters, int err,
+                        float pct, hd_result* out) {
+    // s0 dilates A and covers B (distances of B's voxels); s1 the reverse.
+    hd_result& r = *out;
+    std::memset(&r, 0, sizeof r);
+    r.n_a = I.n_a;
+    r.n_b = I.n_b;
+    r.n_a_not_b = I.n_a - I.n_ab;
+    r.n_b_not_a = I.n_b - I.n_ab;
+    r.iterations = iters;
+    if (I.n_a == 0 && I.n_b == 0) {
+        r.status = HD_OK;
+        return HD_OK;
+    }
+    if (I.n_a == 0 || I.n_b == 0) {
+        r.status = HD_EMPTY_MASK;
+        r.hd = r.hd_ab = r.hd_ba = r.hd_robust = -1;
+        r.avg_hd = std::nan("");
+        return HD_EMPTY_MASK;
+    }
+    int st = err;
+    if (!st) st = s0.status ? s0.status : s1.status;
+    if (!st && (s0.remaining != 0 || s1.remaining != 0)) st = HD_ERR_ITER_LIMIT;
+    r.status = st;
+    r.hd_ba = s0.hd;
+    r.sum_ba = s0.sum;
+    r.hd_ab = s1.hd;
+    r.sum_ab = s1.sum;
+    r.hd = std::max(r.hd_ab, r.hd_ba);
+    r.avg_hd = (double)(r.sum_ab + r.sum_ba) / (double)(r.n_a + r.n_b);
+    r.hd_robust = std::max(robust_k(hist_ab, kp1, r.n_a_not_b, pct), robust_k(hist_ba, kp1, r.n_b_not_a, pct));
+    if (st != HD_OK) r.hd = r.hd_ab = r.hd_ba = r.hd_robust = -1;
+    return (hd_status)st;
+}
+
+void pick_shape(hd_context* ctx, int se, const PairIn* pairs, int n, int* bxw, int* bz, int* cps) {
+    *bxw = 4;
+    *bz = 8;
+    *cps = 0;
+    double vox = 0;
+    for (int i = 0; i < n; ++i) vox += (double)pairs[i].W * pairs[i].H * pairs[i].D;
+    vox /= std::max(1, n);
+    auto it = ctx->tune.entries.find(tune_key(se, vox, n));
+    if (it != ctx->tune.entries.end()) {
+        *bxw = it->second.bxw;
+        *bz = it->second.bz;
+        *cps = it->second.ctas_per_sm;
+    }
+    if (ctx->opt.brick_x_words > 0) *bxw = ctx->opt.brick_x_words;
+    if (ctx->opt.brick_z > 0) *bz = ctx->opt.brick_z;
+    if (ctx->opt.ctas_per_sm > 0) *cps = ctx->opt.ctas_per_sm;
+}
+
+hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s, const RunOpts& ro,
+                    hd_result* out) {
+    if (n <= 0) return HD_OK;
+    if (n > hdk::kMaxPairsPerLaunch) return set_error(ctx, HD_ERR_BAD_ARG, "too many pairs in one launch");
+    const int se = ro.se;
+    int bxw = ro.bxw, bz = ro.bz, cps = ro.ctas_per_sm;
+    {
+        int tb, tz, tc;
+        pick_shape(ctx, se, pairs, n, &tb, &tz, &tc);
+        if (!bxw) bxw = tb;
+        if (!bz) bz = tz;
+        if (!cps) cps = tc;
+    }
+    const void* solve_fn = hdk::solve_kernel_ptr(se, bxw, bz);
+    if (!solve_fn)
+        return set_error(ctx, HD_ERR_BAD_ARG, "brick shape %d words x %d planes not compiled in", bxw, bz);
+    const int by = 32 / bxw;
+    const bool stats = ro.stats != 0;
+
+    // ---- layout --------------------------------------------------------
+    std::vector<PairPlan> plan(n);
+    size_t cur = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = cur;
+        cur = align_up(cur + std::max<size_t>(bytes, 1));
+        return o;
+    };
+    const size_t off_ctl = take(sizeof(Ctl));
+    const size_t off_states = take(sizeof(JobState) * 2 * n);
+    const size_t off_infos = take(sizeof(PairInfo) * n);
+    const size_t off_descs = take(sizeof(PairDesc) * n);
+    const size_t upload_bytes = cur;           // [ctl .. descs]
+    const size_t readback_bytes = off_descs;   // [ctl .. infos]
+    const size_t off_jobs = take(sizeof(Job) * 2 * n);
+    size_t hist_words = 0;
+    unsigned long long total_bricks = 0;
+    int kmax_all = 0;
+    for (int i = 0; i < n; ++i) {
+        PairPlan& q = plan[i];
+        const PairIn& P = pairs[i];
+        q.wxf = (P.W + 31) / 32;
+        q.full_words = (long long)q.wxf * P.H * P.D;
+        const long long pitch = (q.wxf + 3) / 4 * 4;
+        q.dom_words = pitch * P.H * P.D;
+        q.bricks = (long long)((q.wxf + bxw - 1) / bxw) * ((P.H + by - 1) / by) * ((P.D + bz - 1) / bz);
+        int kmax = P.W + P.H + P.D;
+        if (ctx->opt.max_iterations > 0) kmax = std::min(kmax, ctx->opt.max_iterations);
+        q.kmax = kmax;
+        kmax_all = std::max(kmax_all, kmax);
+        q.tiles = (long long)((P.W + 31) / 32) * ((P.H + 31) / 32) * ((P.D + 31) / 32);
+        q.brick0 = total_bricks;
+        total_bricks += 2ULL * (unsigned long long)q.bricks;
+        hist_words += 2ULL * (kmax + 1);
+    }
+    const size_t off_hist = take(sizeof(uint64_t) * hist_words);
+    size_t hcur = 0;
+    for (int i = 0; i < n; ++i) {
+        plan[i].off_hist = off_hist + hcur * sizeof(uint64_t);
+        hcur += 2ULL * (plan[i].kmax + 1);
+    }
+    const size_t qbytes = sizeof(unsigned long long) * std::max<unsigned long long>(total_bricks, 1);
+    const size_t off_q[3] = {take(qbytes), take(qbytes), take(qbytes)};
+    for (int i = 0; i < n; ++i) {
+        PairPlan& q = plan[i];
+        q.off_pa = take(4ULL * q.full_words);
+        q.off_pb = take(4ULL * q.full_words);
+        for (int j = 0; j < 2; ++j)
+            for (int b = 0; b < 3; ++b) q.off_jb[j][b] = take(4ULL * q.dom_words);
+        const size_t nb = (size_t)pairs[i].W * pairs[i].H * pairs[i].D;
+        q.off_in_a = pairs[i].host_a ? take(nb) : 0;
+        q.off_in_b = pairs[i].host_b ? take(nb) : 0;
+        if (stats) {
+            for (int j = 0; j < 2; ++j) {
+                q.off_tstamp[j] = take(sizeof(int32_t) * q.tiles);
+                q.off_tcount[j] = take(sizeof(uint64_t) * (q.kmax + 1));
+            }
+        }
+    }
+    const size_t total_bytes = cur;
+    const size_t pinned_bytes = upload_bytes + sizeof(uint64_t) * (hist_words + (stats ? hist_words : 0));
+
+    cudaError_t e = ctx->arena.ensure(total_bytes);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "device workspace");
+    if (total_bricks > ctx->stamp_slots || ctx->g_next > (1 << 30)) {
+        const size_t want = std::max<size_t>(total_bricks, ctx->stamp_slots);
+        e = ctx->stamps.ensure(sizeof(int32_t) * want);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "brick stamps");
+        e = cudaMemsetAsync(ctx->stamps.ptr, 0, sizeof(int32_t) * want, s);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "stamp reset");
+        ctx->stamp_slots = want;
+        ctx->g_next = 1;
+    }
+    e = ctx->pinned.ensure(pinned_bytes);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "pinned staging");
+
+    char* dbase = (char*)ctx->arena.ptr;
+    char* hbase = (char*)ctx->pinned.ptr;
+    const int g0 = ctx->g_next;
+
+    // ---- host-side descriptors ------------------------------------------
+    std::memset(hbase, 0, upload_bytes);
+    PairInfo* hinfo = (PairInfo*)(hbase + off_infos);
+    PairDesc* hdesc = (PairDesc*)(hbase + off_descs);
+    for (int i = 0; i < n; ++i) {
+        const PairIn& P = pairs[i];
+        const PairPlan& q = plan[i];
+        PairInfo& I = hinfo[i];
+        I.bb[0] = I.bb[2] = I.bb[4] = 0x7fffffff;
+        I.bb[1] = I.bb[3] = I.bb[5] = -1;
+        PairDesc& Dd = hdesc[i];
+        Dd.a = P.host_a ? (const uint8_t*)(dbase + q.off_in_a) : P.a;
+        Dd.b = P.host_b ? (const uint8_t*)(dbase + q.off_in_b) : P.b;
+        Dd.pa = (uint32_t*)(dbase + q.off_pa);
+        Dd.pb = (uint32_t*)(dbase + q.off_pb);
+        for (int j = 0; j < 2; ++j) {
+            for (int b = 0; b < 3; ++b) Dd.jb[j][b] = (uint32_t*)(dbase + q.off_jb[j][b]);
+            Dd.hist[j] = (unsigned long long*)(dbase + q.off_hist) + (size_t)j * (q.kmax + 1);
+            Dd.brick0[j] = q.brick0 + (unsigned long long)j * q.bricks;
+            Dd.tstamp[j] = stats ? (int32_t*)(dbase + q.off_tstamp[j]) : nullptr;
+            Dd.tcount[j] = stats ? (unsigned long long*)(dbase + q.off_tcount[j]) : nullptr;
+        }
+        Dd.W = P.W;
+        Dd.H = P.H;
+        Dd.D = P.D;
+        Dd.wxf = q.wxf;
+        Dd.se = se;
+        Dd.aligned = ((((uintptr_t)Dd.a) | ((uintptr_t)Dd.b)) & 15) == 0;
+        Dd.kmax = q.kmax;
+        Dd.job0 = 2 * i;
+        Dd.info = (PairInfo*)(dbase + off_infos) + i;
+    }
+
+    // ---- uploads ----------------------------------------------------------
+    e = cudaMemcpyAsync(dbase, hbase, upload_bytes, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "descriptor upload");
+    for (int i = 0; i < n; ++i) {
+        const size_t nb = (size_t)pairs[i].W * pairs[i].H * pairs[i].D;
+        if (pairs[i].host_a) {
+            e = cudaMemcpyAsync(dbase + plan[i].off_in_a, pairs[i].host_a, nb, cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "mask upload");
+        }
+        if (pairs[i].host_b) {
+            e = cudaMemcpyAsync(dbase + plan[i].off_in_b, pairs[i].host_b, nb, cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "mask upload");
+        }
+    }
+    if (stats) {
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < 2; ++j) {
+                e = hdk::launch_zero_i32((int32_t*)(dbase + plan[i].off_tstamp[j]), plan[i].tiles, s);
+                if (e == cudaSuccess)
+                    e = cudaMemsetAsync(dbase + plan[i].off_tcount[j], 0,
+                                        sizeof(uint64_t) * (plan[i].kmax + 1), s);
+                if (e != cudaSuccess) return cuda_fail(ctx, e, "instrumentation reset");
+            }
+    }
+
+    // ---- pack, set-up -----------------------------------------------------
+    long long max_words = 0;
+    for (int i = 0; i < n; ++i) max_words = std::max(max_words, plan[i].full_words);
+    const int grid_x = (int)std::min<long long>(1024, std::max<long long>(1, (max_words + 2047) / 2048));
+    const PairDesc* ddesc = (const PairDesc*)(dbase + off_descs);
+    e = hdk::launch_pack(ddesc, n, grid_x, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "pack launch");
+    Ctl* dctl = (Ctl*)(dbase + off_ctl);
+    Job* djobs = (Job*)(dbase + off_jobs);
+    JobState* dstates = (JobState*)(dbase + off_states);
+    unsigned long long* dq[3] = {(unsigned long long*)(dbase + off_q[0]),
+                                 (unsigned long long*)(dbase + off_q[1]),
+                                 (unsigned long long*)(dbase + off_q[2])};
+    e = hdk::launch_setup(ddesc, n, grid_x, djobs, dstates, dq[g0 % 3], dctl, g0, bxw, bz, stats ? 1 : 0, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "setup launch");
+    if (ro.map_a || ro.map_b) {
+        e = hdk::launch_map_init(ddesc, ro.map_a, ro.map_b,
+                                 (long long)pairs[0].W * pairs[0].H * pairs[0].D, s);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "map init launch");
+    }
+
+    // ---- persistent dilation ------------------------------------------------
+    hdk::SolveParams sp{};
+    sp.jobs = djobs;
+    sp.states = dstates;
+    for (int q = 0; q < 3; ++q) sp.queue[q] = dq[q];
+    sp.stamps = (int32_t*)ctx->stamps.ptr;
+    sp.ctl = dctl;
+    sp.map[0] = ro.map_b;  // job 0 covers B
+    sp.map[1] = ro.map_a;  // job 1 covers A
+    sp.map_w = pairs[0].W;
+    sp.map_h = pairs[0].H;
+    sp.map_d = pairs[0].D;
+    sp.g0 = g0;
+    sp.max_iters = kmax_all + 2;
+    sp.stats = stats ? 1 : 0;
+    sp.timeout_ns = ctx->opt.barrier_timeout_ns > 0 ? ctx->opt.barrier_timeout_ns : 10000000000LL;
+    const int occ = occupancy_of(ctx, solve_fn);
+    const int per_sm = cps > 0 ? std::min(cps, occ) : occ;
+    dim3 grid(ctx->sm_count * per_sm), block(256);
+    void* args[] = {&sp};
+    e = cudaLaunchCooperativeKernel(solve_fn, grid, block, args, 0, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "dilation launch");
+
+    // ---- read-back ------------------------------------------------------------
+    e = cudaMemcpyAsync(hbase, dbase, readback_bytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hbase + upload_bytes, dbase + off_hist, sizeof(uint64_t) * hist_words,
+                            cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "result read-back");
+    uint64_t* htc = (uint64_t*)(hbase + upload_bytes) + hist_words;
+    if (stats) {
+        size_t o = 0;
+        for (int i = 0; i < n && e == cudaSuccess; ++i)
+            for (int j = 0; j < 2 && e == cudaSuccess; ++j) {
+                e = cudaMemcpyAsync(htc + o, dbase + plan[i].off_tcount[j], sizeof(uint64_t) * (plan[i].kmax + 1),
+                                    cudaMemcpyDeviceToHost, s);
+                o += plan[i].kmax + 1;
+            }
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "instrumentation read-back");
+    }
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "dilation");
+
+    const Ctl* hctl = (const Ctl*)(hbase + off_ctl);
+    const JobState* hst = (const JobState*)(hbase + off_states);
+    const PairInfo* hin = (const PairInfo*)(hbase + off_infos);
+    const uint64_t* hh = (const uint64_t*)(hbase + upload_bytes);
+    ctx->g_next = std::max(ctx->g_next, hctl->g_end) + 2;
+    const float pct = (ctx->opt.percentile > 0.f && ctx->opt.percentile <= 1.f) ? ctx->opt.percentile : 0.95f;
+    hd_status first = HD_OK;
+    size_t hoff = 0, toff = 0;
+    for (int i = 0; i < n; ++i) {
+        const int kp1 = plan[i].kmax + 1;
+        const uint64_t* hist_ba = hh + hoff;
+        const uint64_t* hist_ab = hh + hoff + kp1;
+        hoff += 2ULL * kp1;
+        if (stats) {
+            const uint64_t* tc0 = htc + toff;
+            const uint64_t* tc1 = htc + toff + kp1;
+            toff += 2ULL * kp1;
+            if (n == 1) {
+                for (int k = 0; k < ro.tiles_len; ++k) {
+                    if (ro.tiles_ba) ro.tiles_ba[k] = k < kp1 ? tc0[k] : 0;
+                    if (ro.tiles_ab) ro.tiles_ab[k] = k < kp1 ? tc1[k] : 0;
+                }
+                if (ro.bricks) *ro.bricks = hst[2 * i].bricks + hst[2 * i + 1].bricks;
+            }
+        }
+        const hd_status st = decode_result(hin[i], hst[2 * i], hst[2 * i + 1], hist_ab, hist_ba, kp1,
+                                           hctl->iters_run, hctl->err, pct, &out[i]);
+        if (st == HD_EMPTY_MASK && first == HD_OK) first = st;
+        if (st != HD_OK && st != HD_EMPTY_MASK) {
+            if (first == HD_OK || first == HD_EMPTY_MASK) first = st;
+            set_error(ctx, st, "pair %d: %s", i, hd_status_string(st));
+        }
+    }
+    return first;
+}
+
+}  // namespace hdh
+
+// ============================================================================
+// C ABI
+// ============================================================================
+using namespace hdh;
+
+namespace hdk {
+const void* solve_kernel_ptr(int se, int bxw, int bz) {
+    return se == 0 ? solve_kernel_ptr_se6(bxw, bz) : solve_kernel_ptr_se18(bxw, bz);
+}
+}  // namespace hdk
+
+extern "C" {
+
+void hd_options_init(hd_options* opt) {
+    if (!opt) return;
+    std::memset(opt, 0, sizeof *opt);
+    opt->percentile = 0.95f;
+    opt->zero_copy = 1;
+}
+
+const char* hd_status_string(hd_status s) {
+    switch (s) {
+        case HD_OK: return "ok";
+        case HD_EMPTY_MASK: return "exactly one mask is empty";
+        case HD_ERR_BAD_ARG: return "bad argument";
+        case HD_ERR_OOM: return "out of memory";
+        case HD_ERR_CUDA: return "CUDA error";
+        case HD_ERR_TIMEOUT: return "device wait timed out";
+        case HD_ERR_CANCELLED: return "cancelled";
+        case HD_ERR_ITER_LIMIT: return "iteration limit reached";
+        case HD_ERR_NOT_READY: return "not ready";
+        case HD_ERR_UNSUPPORTED: return "unsupported";
+        case HD_ERR_BUSY: return "server queue full";
+    }
+    return "unknown status";
+}
+
+const char* hd_version(void) { return "hd_gb300 1.0 sm_103a"; }
+
+hd_status hd_context_create(int device, const hd_options* opt, hd_context** out) {
+    if (!out) return HD_ERR_BAD_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return HD_ERR_CUDA;
+    }
+    if (device < 0 || device >= ndev) return HD_ERR_BAD_ARG;
+    hd_context* ctx = new (std::nothrow) hd_context();
+    if (!ctx) return HD_ERR_OOM;
+    ctx->device = device;
+    hd_options_init(&ctx->opt);
+    if (opt) ctx->opt = *opt;
+    if (opt && opt->tuning_table) ctx->tuning_path = opt->tuning_table;
+    ctx->opt.tuning_table = nullptr;
+    {
+        DeviceGuard g(device);
+        if (!g.ok) {
+            delete ctx;
+            return HD_ERR_CUDA;
+        }
+        e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+        int coop = 0;
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+        int ats = 0;
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+        if (e != cudaSuccess || !coop) {
+            cudaGetLastError();
+            if (ctx->stream) cudaStreamDestroy(ctx->stream);
+            delete ctx;
+            return HD_ERR_CUDA;
+        }
+        ctx->pageable_ats = ats;
+    }
+    if (!ctx->tuning_path.empty()) ctx->tune.load(ctx->tuning_path);
+    *out = ctx;
+    return HD_OK;
+}
+
+hd_status hd_context_destroy(hd_context* ctx) {
+    if (!ctx) return HD_ERR_BAD_ARG;
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        DeviceGuard g(ctx->device);
+        if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+        ctx->arena.release();
+        ctx->stamps.release();
+        ctx->pinned.release();
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
+        ctx->stream = nullptr;
+    }
+    delete ctx;
+    return HD_OK;
+}
+
+const char* hd_context_last_error(hd_context* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+static hd_status metric_to_se(hd_context* ctx, int metric, int* se) {
+    if (metric == HD_SE6) *se = 0;
+    else if (metric == HD_SE18_FORBENCH) *se = 1;
+    else return set_error(ctx, HD_ERR_BAD_ARG, "unknown metric %d", metric);
+    return HD_OK;
+}
+
+hd_status hd_compute_u8(hd_context* ctx, const uint8_t* a, const uint8_t* b, int32_t W, int32_t H,
+                        int32_t D, hd_metric metric, hd_result* out) {
+    if (!ctx || !a || !b || !out) return HD_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    int se = 0;
+    hd_status st = metric_to_se(ctx, metric, &se);
+    if (st == HD_OK) st = check_dims(ctx, W, H, D);
+    if (st != HD_OK) return st;
+    DeviceGuard g(ctx->device);
+    if (!g.ok) return set_error(ctx, HD_ERR_CUDA, "cannot select device %d", ctx->device);
+    PairIn p{a, b, W, H, D, nullptr, nullptr};
+    if (ctx->opt.zero_copy) {
+        p.a = zero_copy_ptr(ctx, a);
+        p.b = zero_copy_ptr(ctx, b);
+    } else {
+        p.a = p.b = nullptr;
+    }
+    if (!p.a) p.host_a = a;
+    if (!p.b) p.host_b = b;
+    RunOpts ro;
+    ro.se = se;
+    return run_pairs(ctx, &p, 1, ctx->stream, ro, out);
+}
+
+hd_status hd_compute_u8_device(hd_context* ctx, const uint8_t* d_a, const uint8_t* d_b, int32_t W,
+                               int32_t H, int32_t D, hd_metric metric, void* stream, hd_result* out) {
+    if (!ctx || !d_a || !d_b || !out) return HD_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    int se = 0;
+    hd_status st = metric_to_se(ctx, metric, &se);
+    if (st == HD_OK) st = check_dims(ctx, W, H, D);
+    if (st != HD_OK) return st;
+    DeviceGuard g(ctx->device);
+    if (!g.ok) return set_error(ctx, HD_ERR_CUDA, "cannot select device %d", ctx->device);
+    PairIn p{d_a, d_b, W, H, D, nullptr, nullptr};
+    RunOpts ro;
+    ro.se = se;
+    return run_pairs(ctx, &p, 1, stream ? (cudaStream_t)stream : ctx->stream, ro, out);
+}
+
+hd_status hd_batch_compute(hd_context* ctx, const hd_pair_desc* pairs, int32_t n, hd_result* out) {
+    if (!ctx || (n > 0 && (!pairs || !out)) || n < 0) return HD_ERR_BAD_ARG;
+    if (n == 0) return HD_OK;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    for (int i = 0; i < n; ++i) {
+        int se;
+        if (!pairs[i].a || !pairs[i].b) return set_error(ctx, HD_ERR_BAD_ARG, "pair %d: null mask", i);
+        hd_status st = metric_to_se(ctx, pairs[i].metric, &se);
+        if (st == HD_OK) st = check_dims(ctx, pairs[i].W, pairs[i].H, pairs[i].D);
+        if (st != HD_OK) return st;
+    }
+    DeviceGuard g(ctx->device);
+    if (!g.ok) return set_error(ctx, HD_ERR_CUDA, "cannot select device %d", ctx->device);
+    hd_status first = HD_OK;
+    for (int se = 0; se < 2; ++se) {
+        std::vector<PairIn> in;
+        std::vector<int> idx;
+        for (int i = 0; i < n; ++i) {
+            const int pse = pairs[i].metric == HD_SE6 ? 0 : 1;
+            if (pse != se) continue;
+            PairIn p{pairs[i].a, pairs[i].b, pairs[i].W, pairs[i].H, pairs[i].D, nullptr, nullptr};
+            if (!pairs[i].on_device) {
+                p.a = ctx->opt.zero_copy ? zero_copy_ptr(ctx, pairs[i].a) : nullptr;
+                p.b = ctx->opt.zero_copy ? zero_copy_ptr(ctx, pairs[i].b) : nullptr;
+                if (!p.a) p.host_a = pairs[i].a;
+                if (!p.b) p.host_b = pairs[i].b;
+            }
+            in.push_back(p);
+            idx.push_back(i);
+        }
+        if (in.empty()) continue;
+        std::vector<hd_result> res(in.size());
+        RunOpts ro;
+        ro.se = se;
+        const hd_status st = run_pairs(ctx, in.data(), (int)in.size(), ctx->stream, ro, res.data());
+        for (size_t j = 0; j < idx.size(); ++j) out[idx[j]] = res[j];
+        if (st != HD_OK && st != HD_EMPTY_MASK) return st;
+        if (first == HD_OK) first = st;
+    }
+    return first;
+}
+
+hd_status hd_profile_u8_device(hd_context* ctx, const uint8_t* d_a, const uint8_t* d_b, int32_t W,
+                               int32_t H, int32_t D, hd_metric metric, hd_result* out,
+                               uint64_t* tiles_ab, uint64_t* tiles_ba, int32_t len,
+                               uint64_t* bricks_processed) {
+    if (!ctx || !d_a || !d_b || !out || len < 0) return HD_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    int se = 0;
+    hd_status st = metric_to_se(ctx, metric, &se);
+    if (st == HD_OK) st = check_dims(ctx, W, H, D);
+    if (st != HD_OK) return st;
+    DeviceGuard g(ctx->device);
+    if (!g.ok) return set_error(ctx, HD_ERR_CUDA, "cannot select device %d", ctx->device);
+    PairIn p{d_a, d_b, W, H, D, nullptr, nullptr};
+    RunOpts ro;
+    ro.se = se;
+    ro.stats = 1;
+    ro.tiles_ab = tiles_ab;
+    ro.tiles_ba = tiles_ba;
+    ro.tiles_len = len;
+    ro.bricks = bricks_processed;
+    return run_pairs(ctx, &p, 1, ctx->stream, ro, out);
+}
+
+hd_status hd_distance_map_device(hd_context* ctx, const uint8_t* d_a, const uint8_t* d_b, int32_t W,
+                                 int32_t H, int32_t D, hd_metric metric, int32_t* d_map_a,
+                                 int32_t* d_map_b, hd_result* out) {
+    if (!ctx || !d_a || !d_b || !out || !d_map_a || !d_map_b) return HD_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    int se = 0;
+    hd_status st = metric_to_se(ctx, metric, &se);
+    if (st == HD_OK) st = check_dims(ctx, W, H, D);
+    if (st != HD_OK) return st;
+    DeviceGuard g(ctx->device);
+    if (!g.ok) return set_error(ctx, HD_ERR_CUDA, "cannot select device %d", ctx->device);
+    PairIn p{d_a, d_b, W, H, D, nullptr, nullptr};
+    RunOpts ro;
+    ro.se = se;
+    ro.map_a = d_map_a;
+    ro.map_b = d_map_b;
+    return run_pairs(ctx, &p, 1, ctx->stream, ro, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,108 @@
+// hd_device.cuh -- device-side data structures shared by the packing, set-up
+// and dilation kernels and by the host orchestration.
+//
+// Layout in HBM (one pair):
+//   a, b        uint8 masks, W x H x D, x fastest (caller's or staged copy)
+//   pa, pb      the full volume bit-packed along x: 32 voxels per uint32,
+//               bit i of word w of row (y, z) is voxel x = 32 w + i;
+//               row = wxf = ceil(W / 32) words, index (z * H + y) * wxf + w
+//   per direction (a "job": dilate a source mask until it covers a target):
+//     buf[0], buf[1]  ping-pong dilation state over the job's domain
+//     U               target voxels not yet covered
+//               domain layout [z][y][pitch] words, pitch = ceil(wx / 4) * 4,
+//               pad words zero.  The domain is the bounding box of A u B with
+//               x widened to whole words (6-neighbour element) or the whole
+//               volume (18-neighbour element).
+//   bricks      the unit of work: BXW words (x) x (32 / BXW) rows (y) x BZ
+//               planes (z), one warp per brick, lane (lx, ly) owns one word
+//               column and walks z.
+#pragma once
+#include <stdint.h>
+
+namespace hdk {
+
+constexpr int kMaxPairsPerLaunch = 65535;
+
+// Bounding box and counts of one pair, accumulated by the packing kernel.
+struct PairInfo {
+    unsigned long long n_a, n_b, n_ab;
+    int32_t bb[6];  // min x, max x, min y, max y, min z, max z (min = INT_MAX, max = -1 when empty)
+    int32_t pad[2];
+};
+
+// Packing / set-up descriptor of one pair (host-written).
+struct PairDesc {
+    const uint8_t* a;
+    const uint8_t* b;
+    uint32_t* pa;      // full packed A, wxf * H * D words
+    uint32_t* pb;
+    uint32_t* jb[2][3];  // per job: buf0, buf1, U (capacity: pitch_full * H * D words each)
+    unsigned long long* hist[2];  // per job: kmax + 1 counters
+    int32_t W, H, D, wxf;
+    int32_t se;          // 0: 6-neighbour, 1: 18-neighbour (forBench default)
+    int32_t aligned;     // a and b are 16-byte aligned
+    int32_t kmax;        // iteration cap per job
+    int32_t job0;        // index of this pair's first job (jobs 2p, 2p+1)
+    unsigned long long brick0[2];  // first global brick id of each job
+    PairInfo* info;
+    int32_t* tstamp[2];            // instrumented runs only (else null)
+    unsigned long long* tcount[2];
+};
+
+// One direction of a pair, written by the set-up kernel.
+struct Job {
+    uint32_t* buf[2];
+    uint32_t* U;
+    unsigned long long* hist;  // newly covered voxels per local step
+    int32_t wv, h, d;          // domain size in voxels
+    int32_t wx, pitch;         // words per row, row pitch (words)
+    uint32_t tailmask;         // valid bits of a row's last word
+    int32_t nbx, nby, nbz;     // brick grid
+    int32_t k0;                // global iteration at which local step 1 runs
+    int32_t kmax;              // local step cap
+    int32_t ox, oy, oz;        // domain origin in the full volume (voxels)
+    int32_t tw, th;            // full-volume 32^3 tile grid (x, y), instrumented runs
+    unsigned long long brick0;
+    int32_t* tstamp;           // instrumented runs: per full-volume tile, last marked step
+    unsigned long long* tcount;  // instrumented runs: tiles per step
+};
+
+// Mutable per-job state.
+struct JobState {
+    unsigned long long sum;        // sum over covered target voxels of their step
+    unsigned long long remaining;  // target voxels not yet covered
+    unsigned long long bricks;     // bricks processed (instrumented runs)
+    int32_t hd;                    // last step that covered something
+    int32_t last_k;                // last local step run
+    int32_t status;                // 0 ok, else hd_status
+    int32_t active;                // 1 while the job takes part in the dilation loop
+};
+
+// Loop control shared by all CTAs of the persistent kernel.
+struct Ctl {
+    unsigned int bar_count;
+    unsigned int bar_gen;
+    int32_t err;           // first error (hd_status), 0 = none
+    int32_t jobs_active;   // jobs with uncovered target voxels
+    unsigned int qcount[3];
+    int32_t cont[2];       // continue flag decided by the last CTA at each barrier (by parity)
+    int32_t g_end;         // next global iteration (written at exit)
+    int32_t iters_run;
+    int32_t pad[5];
+};
+
+struct SolveParams {
+    Job* jobs;
+    JobState* states;
+    unsigned long long* queue[3];  // entries (job << 32) | local brick
+    int32_t* stamps;               // per global brick: last iteration it was queued for
+    Ctl* ctl;
+    int32_t* map[2];               // optional dense per-voxel distance maps (per pair: job 0 / 1)
+    int32_t map_w, map_h, map_d;   // full-volume sizes for the maps
+    int32_t g0;                    // first global iteration of this launch
+    int32_t max_iters;             // iterations this launch may run
+    int32_t stats;                 // instrumented run
+    long long timeout_ns;          // one barrier wait
+};
+
+}  // namespace hdk

@@ -1,0 +1,26 @@
+// hd_kernels.h -- launch wrappers of the device kernels, for the host
+// orchestration in hd_api.cu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "hd_device.cuh"
+
+namespace hdk {
+
+cudaError_t launch_pack(const PairDesc* d_descs, int npairs, int grid_x, cudaStream_t s);
+cudaError_t launch_setup(const PairDesc* d_descs, int npairs, int grid_x, Job* jobs, JobState* states,
+                         unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int bz, int stats,
+                         cudaStream_t s);
+cudaError_t launch_zero_i32(int32_t* p, long long n, cudaStream_t s);
+cudaError_t launch_map_init(const PairDesc* d_descs, int32_t* map_a, int32_t* map_b, long long n,
+                            cudaStream_t s);
+
+// The persistent dilation kernel for one (element, brick width, brick depth).
+// Returns the kernel's host stub for cudaLaunchCooperativeKernel, or nullptr
+// if that shape is not compiled in.  Compiled shapes: bxw in {2, 4, 8},
+// bz in {4, 8, 16}, both elements.
+const void* solve_kernel_ptr(int se, int bxw, int bz);
+const void* solve_kernel_ptr_se6(int bxw, int bz);
+const void* solve_kernel_ptr_se18(int bxw, int bz);
+
+}  // namespace hdk

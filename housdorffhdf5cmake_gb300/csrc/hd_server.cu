@@ -1,0 +1,619 @@
+// hd_server.cu -- continuous-batching request loop.
+//
+// No counterpart in the reference (it computes one pair per call).  Requests
+// are admitted while device memory (a byte budget) and job slots allow; an
+// admitted pair is packed and set up on the device and its two jobs join the
+// resident persistent dilation loop at the next "tick" with their own step
+// counter (Job::k0), so pairs that arrive while others are mid-flight overlap
+// on the device.  A tick is one cooperative launch of the same dilation kernel
+// as the single-pair path, bounded to tick_iterations steps; between ticks the
+// scheduler thread reads the jobs' states, completes finished pairs, frees
+// their memory and admits waiting ones.  Each pair's result depends only on
+// its own masks, so it is identical alone and in any mix.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "hd/hd.h"
+#include "hd_internal.h"
+#include "hd_kernels.h"
+
+using namespace hdh;
+using hdk::Ctl;
+using hdk::Job;
+using hdk::JobState;
+using hdk::PairDesc;
+using hdk::PairInfo;
+
+namespace {
+
+enum ReqState { kWaiting = 0, kResident = 1, kDone = 2 };
+
+struct Request {
+    uint64_t ticket = 0;
+    int32_t W = 0, H = 0, D = 0;
+    const uint8_t* dev_a = nullptr;  // caller's device masks (on_device)
+    const uint8_t* dev_b = nullptr;
+    std::vector<uint8_t> host_a, host_b;  // copies of host masks
+    ReqState state = kWaiting;
+    bool cancel = false;
+    hd_result result{};
+    // resident resources
+    int slot = -1;
+    void* resident = nullptr;   // job buffers + histograms + info
+    size_t resident_bytes = 0;
+    size_t transient_bytes = 0;
+    unsigned long long brick0 = 0, nbricks = 0;  // per job
+    int kmax = 0;
+    int wxf = 0;
+    long long dom_words = 0;
+    size_t off_hist = 0, off_info = 0;
+};
+
+// First-fit allocator over [0, cap) (brick ids).
+struct RangeAlloc {
+    std::map<unsigned long long, unsigned long long> free_;  // start -> length
+    explicit RangeAlloc(unsigned long long cap = 0) {
+        if (cap) free_[0] = cap;
+    }
+    bool alloc(unsigned long long n, unsigned long long* out) {
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= n) {
+                *out = it->first;
+                const unsigned long long s = it->first + n, l = it->second - n;
+                free_.erase(it);
+                if (l) free_[s] = l;
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(unsigned long long s, unsigned long long n) {
+        auto it = free_.emplace(s, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+};
+
+inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+struct hd_server {
+    hd_context* ctx = nullptr;
+    hd_server_options opt{};
+    int se = 0, bxw = 4, bz = 8, grid = 0;
+    const void* solve_fn = nullptr;
+    cudaStream_t stream = nullptr;
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv;       // wakes the scheduler
+    std::condition_variable done_cv;  // wakes waiters
+    bool stop = false;
+    uint64_t next_ticket = 1;
+    std::deque<Request*> waiting;
+    std::map<uint64_t, std::unique_ptr<Request>> reqs;
+    std::vector<Request*> slots;      // resident pair per slot
+    std::vector<int> free_slots;
+    std::vector<int> quarantine;      // slots freed during the last tick
+    RangeAlloc bricks;
+    unsigned long long brick_cap = 0;
+    // persistent device state
+    Job* d_jobs = nullptr;
+    JobState* d_states = nullptr;
+    Ctl* d_ctl = nullptr;
+    unsigned long long* d_queue[3] = {nullptr, nullptr, nullptr};
+    int32_t* d_stamps = nullptr;
+    PairDesc* d_descs = nullptr;      // per-tick admission descriptors
+    int max_admit = 64;
+    void* h_pinned = nullptr;         // descriptors out, states in
+    size_t h_pinned_bytes = 0;
+    int g_next = 1;
+    hd_server_stats stats{};
+    std::string err;
+};
+
+namespace {
+
+hd_status cuda_err(hd_server* s, cudaError_t e, const char* where) {
+    s->err = std::string(where) + ": " + cudaGetErrorString(e);
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? HD_ERR_OOM : HD_ERR_CUDA;
+}
+
+// Sizes of one request's device memory (resident part lives until completion,
+// transient part only through packing and set-up).
+void plan_request(hd_server* s, Request* r) {
+    const int by = 32 / s->bxw;
+    r->wxf = (r->W + 31) / 32;
+    const long long pitch = (r->wxf + 3) / 4 * 4;
+    r->dom_words = pitch * r->H * r->D;
+    r->nbricks = (unsigned long long)((r->wxf + s->bxw - 1) / s->bxw) * ((r->H + by - 1) / by) *
+                 ((r->D + s->bz - 1) / s->bz);
+    r->kmax = r->W + r->H + r->D;
+    const size_t job_bytes = align_up(4ULL * r->dom_words);
+    r->off_hist = 6 * job_bytes;
+    r->off_info = align_up(r->off_hist + 2ULL * (r->kmax + 1) * sizeof(uint64_t));
+    r->resident_bytes = align_up(r->off_info + sizeof(PairInfo));
+    const size_t nb = (size_t)r->W * r->H * r->D;
+    const size_t packed = align_up(4ULL * r->wxf * r->H * r->D);
+    r->transient_bytes = 2 * packed + (r->dev_a ? 0 : 2 * align_up(nb));
+}
+
+void complete(hd_server* s, Request* r, hd_status st) {
+    r->state = kDone;
+    r->result.status = st;
+    if (st != HD_OK && st != HD_EMPTY_MASK) r->result.hd = -1;
+    s->stats.completed += 1;
+}
+
+// One scheduler tick.  Called with the server lock NOT held.
+void tick(hd_server* s) {
+    std::vector<Request*> admit;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        // cancelled waiting requests leave at once
+        for (auto it = s->waiting.begin(); it != s->waiting.end();) {
+            if ((*it)->cancel) {
+                (*it)->result.status = HD_ERR_CANCELLED;
+                (*it)->state = kDone;
+                s->stats.cancelled += 1;
+                it = s->waiting.erase(it);
+            } else {
+                ++it;
+            }
+        }
+        for (int q : s->quarantine) s->free_slots.push_back(q);
+        s->quarantine.clear();
+        while (!s->waiting.empty() && (int)admit.size() < s->max_admit && !s->free_slots.empty()) {
+            Request* r = s->waiting.front();
+            const size_t need = r->resident_bytes + r->transient_bytes;
+            if (need > s->opt.hbm_budget_bytes) {  // can never fit
+                s->waiting.pop_front();
+                r->result.status = HD_ERR_OOM;
+                r->state = kDone;
+                s->stats.completed += 1;
+                continue;
+            }
+            if (s->stats.bytes_in_use + need > s->opt.hbm_budget_bytes) break;
+            unsigned long long b0 = 0;
+            if (!s->bricks.alloc(2 * r->nbricks, &b0)) break;
+            s->waiting.pop_front();
+            r->brick0 = b0;
+            r->slot = s->free_slots.back();
+            s->free_slots.pop_back();
+            s->slots[r->slot] = r;
+            r->state = kResident;
+            s->stats.bytes_in_use += need;
+            s->stats.bytes_peak = std::max(s->stats.bytes_peak, s->stats.bytes_in_use);
+            admit.push_back(r);
+        }
+        s->done_cv.notify_all();
+    }
+    cudaStream_t st = s->stream;
+    cudaError_t e = cudaSuccess;
+    // ---- admission: allocate, upload, pack, set up --------------------------
+    std::vector<void*> transient(admit.size(), nullptr);
+    std::vector<PairDesc> descs;
+    std::vector<Request*> admitted;
+    for (size_t i = 0; i < admit.size(); ++i) {
+        Request* r = admit[i];
+        void* res = nullptr;
+        void* tr = nullptr;
+        e = cudaMallocAsync(&res, r->resident_bytes, st);
+        if (e == cudaSuccess) e = cudaMallocAsync(&tr, r->transient_bytes, st);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            if (res) cudaFreeAsync(res, st);
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->stats.bytes_in_use -= r->resident_bytes + r->transient_bytes;
+            s->bricks.release(r->brick0, 2 * r->nbricks);
+            s->slots[r->slot] = nullptr;
+            s->quarantine.push_back(r->slot);
+            complete(s, r, HD_ERR_OOM);
+            continue;
+        }
+        r->resident = res;
+        transient[i] = tr;
+        char* rb = (char*)res;
+        char* tb = (char*)tr;
+        const size_t nb = (size_t)r->W * r->H * r->D;
+        const size_t packed = align_up(4ULL * r->wxf * r->H * r->D);
+        PairDesc d{};
+        if (r->dev_a) {
+            d.a = r->dev_a;
+            d.b = r->dev_b;
+        } else {
+            uint8_t* ia = (uint8_t*)(tb + 2 * packed);
+            uint8_t* ib = ia + align_up(nb);
+            cudaMemcpyAsync(ia, r->host_a.data(), nb, cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(ib, r->host_b.data(), nb, cudaMemcpyHostToDevice, st);
+            d.a = ia;
+            d.b = ib;
+        }
+        d.pa = (uint32_t*)tb;
+        d.pb = (uint32_t*)(tb + packed);
+        const size_t job_bytes = align_up(4ULL * r->dom_words);
+        for (int j = 0; j < 2; ++j) {
+            for (int b = 0; b < 3; ++b) d.jb[j][b] = (uint32_t*)(rb + (3 * j + b) * job_bytes);
+            d.hist[j] = (unsigned long long*)(rb + r->off_hist) + (size_t)j * (r->kmax + 1);
+            d.brick0[j] = r->brick0 + (unsigned long long)j * r->nbricks;
+        }
+        d.W = r->W;
+        d.H = r->H;
+        d.D = r->D;
+        d.wxf = r->wxf;
+        d.se = s->se;
+        d.aligned = ((((uintptr_t)d.a) | ((uintptr_t)d.b)) & 15) == 0;
+        d.kmax = r->kmax;
+        d.job0 = 2 * r->slot;
+        d.info = (PairInfo*)(rb + r->off_info);
+        descs.push_back(d);
+        admitted.push_back(r);
+    }
+    if (!admitted.empty()) {
+        // info initial values, then descriptors
+        std::vector<PairInfo> init(admitted.size());
+        for (auto& I : init) {
+            std::memset(&I, 0, sizeof I);
+            I.bb[0] = I.bb[2] = I.bb[4] = 0x7fffffff;
+            I.bb[1] = I.bb[3] = I.bb[5] = -1;
+        }
+        char* hp = (char*)s->h_pinned + align_up(sizeof(Ctl)) + align_up(sizeof(JobState) * 2 * s->slots.size());
+        std::memcpy(hp, descs.data(), sizeof(PairDesc) * descs.size());
+        e = cudaMemcpyAsync(s->d_descs, hp, sizeof(PairDesc) * descs.size(), cudaMemcpyHostToDevice, st);
+        for (size_t i = 0; i < admitted.size() && e == cudaSuccess; ++i)
+            e = cudaMemcpyAsync(descs[i].info, &init[i], sizeof(PairInfo), cudaMemcpyHostToDevice, st);
+        long long max_words = 0;
+        for (auto* r : admitted) max_words = std::max(max_words, (long long)r->wxf * r->H * r->D);
+        const int gx = (int)std::min<long long>(1024, std::max<long long>(1, (max_words + 2047) / 2048));
+        if (e == cudaSuccess) e = hdk::launch_pack(s->d_descs, (int)admitted.size(), gx, st);
+        if (e == cudaSuccess)
+            e = hdk::launch_setup(s->d_descs, (int)admitted.size(), gx, s->d_jobs, s->d_states,
+                                  s->d_queue[s->g_next % 3], s->d_ctl, s->g_next, s->bxw, s->bz, 0, st);
+        // pageable sources of cudaMemcpyAsync and the info initialisers must
+        // outlive the copies: wait for the admission work before going on
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            cuda_err(s, e, "admission");
+        }
+    }
+    for (void* tr : transient)
+        if (tr) cudaFreeAsync(tr, st);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (auto* r : admitted) s->stats.bytes_in_use -= r->transient_bytes;
+    }
+    // ---- one tick of the persistent dilation loop ---------------------------
+    int resident = 0;
+    for (auto* r : s->slots) resident += r != nullptr;
+    if (resident > 0 && e == cudaSuccess) {
+        hdk::SolveParams sp{};
+        sp.jobs = s->d_jobs;
+        sp.states = s->d_states;
+        for (int q = 0; q < 3; ++q) sp.queue[q] = s->d_queue[q];
+        sp.stamps = s->d_stamps;
+        sp.ctl = s->d_ctl;
+        sp.g0 = s->g_next;
+        sp.max_iters = s->opt.tick_iterations;
+        sp.timeout_ns = s->ctx->opt.barrier_timeout_ns > 0 ? s->ctx->opt.barrier_timeout_ns : 10000000000LL;
+        void* args[] = {&sp};
+        e = cudaLaunchCooperativeKernel(s->solve_fn, dim3(s->grid), dim3(256), args, 0, st);
+    }
+    // ---- read back states, complete finished pairs ---------------------------
+    const size_t nst = 2 * s->slots.size();
+    char* hp = (char*)s->h_pinned;
+    Ctl* hctl = (Ctl*)hp;
+    JobState* hst = (JobState*)(hp + align_up(sizeof(Ctl)));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hctl, s->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hst, s->d_states, sizeof(JobState) * nst, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    int hard_err = 0;
+    if (e != cudaSuccess) {
+        cuda_err(s, e, "tick");
+        hard_err = HD_ERR_CUDA;
+    } else {
+        if (resident > 0) s->g_next = std::max(s->g_next, hctl->g_end);
+        hard_err = hctl->err;
+    }
+    std::vector<Request*> finished;
+    for (size_t sl = 0; sl < s->slots.size(); ++sl) {
+        Request* r = s->slots[sl];
+        if (!r) continue;
+        const JobState& s0 = hst[2 * sl];
+        const JobState& s1 = hst[2 * sl + 1];
+        const bool fin = hard_err != 0 || r->cancel || (s0.active == 0 && s1.active == 0);
+        if (fin) finished.push_back(r);
+    }
+    unsigned long long cancelled_active = 0;
+    for (Request* r : finished) {
+        const size_t sl = (size_t)r->slot;
+        const JobState s0 = hst[2 * sl], s1 = hst[2 * sl + 1];
+        hd_status st_r = HD_OK;
+        if (r->cancel) {
+            st_r = HD_ERR_CANCELLED;
+            cancelled_active += (s0.active != 0) + (s1.active != 0);
+            r->result = hd_result{};
+        } else {
+            const int kp1 = r->kmax + 1;
+            std::vector<uint64_t> hist(2 * kp1);
+            PairInfo info{};
+            cudaError_t e2 = cudaMemcpyAsync(hist.data(), (char*)r->resident + r->off_hist,
+                                             sizeof(uint64_t) * 2 * kp1, cudaMemcpyDeviceToHost, st);
+            if (e2 == cudaSuccess)
+                e2 = cudaMemcpyAsync(&info, (char*)r->resident + r->off_info, sizeof info, cudaMemcpyDeviceToHost, st);
+            if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(st);
+            const float pct = (s->ctx->opt.percentile > 0.f && s->ctx->opt.percentile <= 1.f) ? s->ctx->opt.percentile : 0.95f;
+            if (e2 != cudaSuccess) {
+                cudaGetLastError();
+                st_r = HD_ERR_CUDA;
+            } else {
+                st_r = decode_result(info, s0, s1, hist.data() + kp1, hist.data(), kp1, 0, hard_err, pct, &r->result);
+            }
+        }
+        cudaFreeAsync(r->resident, st);
+        r->resident = nullptr;
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stats.bytes_in_use -= r->resident_bytes;
+        s->bricks.release(r->brick0, 2 * r->nbricks);
+        s->slots[sl] = nullptr;
+        s->quarantine.push_back((int)sl);
+        if (r->cancel) {
+            r->result.status = HD_ERR_CANCELLED;
+            r->state = kDone;
+            s->stats.cancelled += 1;
+        } else {
+            complete(s, r, st_r);
+        }
+    }
+    if (cancelled_active || hard_err) {
+        // Cancelled jobs leave the loop: mark them inactive and fix the
+        // active-job count (no kernel runs between ticks).  After a device
+        // error every resident pair has failed: reset the loop state.
+        if (hard_err) {
+            Ctl z{};
+            cudaMemcpyAsync(s->d_ctl, &z, sizeof z, cudaMemcpyHostToDevice, st);
+            s->g_next += 2;
+        } else {
+            for (Request* r : finished) {
+                if (!r->cancel) continue;
+                JobState off{};
+                const size_t sl = (size_t)r->slot;
+                cudaMemcpyAsync(s->d_states + 2 * sl, &off, sizeof off, cudaMemcpyHostToDevice, st);
+                cudaMemcpyAsync(s->d_states + 2 * sl + 1, &off, sizeof off, cudaMemcpyHostToDevice, st);
+            }
+            Ctl c = *hctl;
+            c.jobs_active -= (int)cancelled_active;
+            cudaMemcpyAsync(&s->d_ctl->jobs_active, &c.jobs_active, sizeof(int32_t), cudaMemcpyHostToDevice, st);
+        }
+        cudaStreamSynchronize(st);
+    }
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stats.ticks += 1;
+        s->done_cv.notify_all();
+    }
+}
+
+void worker_main(hd_server* s) {
+    DeviceGuard g(s->ctx->device);
+    for (;;) {
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            s->cv.wait(lk, [&] {
+                if (s->stop) return true;
+                if (!s->waiting.empty()) return true;
+                for (auto* r : s->slots)
+                    if (r) return true;
+                return false;
+            });
+            if (s->stop) return;
+        }
+        tick(s);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+void hd_server_options_init(hd_server_options* opt) {
+    if (!opt) return;
+    std::memset(opt, 0, sizeof *opt);
+    opt->hbm_budget_bytes = 120ULL << 30;
+    opt->max_queue = 4096;
+    opt->tick_iterations = 16;
+    opt->metric = HD_SE6;
+}
+
+hd_status hd_server_create(hd_context* ctx, const hd_server_options* opt, hd_server** out) {
+    if (!ctx || !out) return HD_ERR_BAD_ARG;
+    *out = nullptr;
+    auto* s = new (std::nothrow) hd_server();
+    if (!s) return HD_ERR_OOM;
+    s->ctx = ctx;
+    hd_server_options_init(&s->opt);
+    if (opt) s->opt = *opt;
+    if (!s->opt.hbm_budget_bytes) s->opt.hbm_budget_bytes = 120ULL << 30;
+    if (s->opt.max_queue <= 0) s->opt.max_queue = 4096;
+    if (s->opt.tick_iterations <= 0) s->opt.tick_iterations = 16;
+    if (s->opt.metric != HD_SE6 && s->opt.metric != HD_SE18_FORBENCH) {
+        delete s;
+        return HD_ERR_BAD_ARG;
+    }
+    s->se = s->opt.metric == HD_SE6 ? 0 : 1;
+    int slots = s->opt.max_inflight > 0 ? s->opt.max_inflight : 1024;
+    slots = std::min(slots, 16384);
+    {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        DeviceGuard g(ctx->device);
+        if (!g.ok) {
+            delete s;
+            return HD_ERR_CUDA;
+        }
+        PairIn typical{nullptr, nullptr, 256, 256, 160, nullptr, nullptr};
+        int cps = 0;
+        pick_shape(ctx, s->se, &typical, 16, &s->bxw, &s->bz, &cps);
+        s->solve_fn = hdk::solve_kernel_ptr(s->se, s->bxw, s->bz);
+        if (!s->solve_fn) {
+            delete s;
+            return HD_ERR_BAD_ARG;
+        }
+        const int occ = occupancy_of(ctx, s->solve_fn);
+        s->grid = ctx->sm_count * (cps > 0 ? std::min(cps, occ) : occ);
+        // brick ids: one per 3 KB of budget (a job brick holds 3 x 1 KB words), capped
+        s->brick_cap = std::min<unsigned long long>(s->opt.hbm_budget_bytes / 3072ULL, 1ULL << 26);
+        s->bricks = RangeAlloc(s->brick_cap);
+        cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_jobs, sizeof(Job) * 2 * slots);
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_states, sizeof(JobState) * 2 * slots);
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_ctl, sizeof(Ctl));
+        for (int q = 0; q < 3 && e == cudaSuccess; ++q)
+            e = cudaMalloc(&s->d_queue[q], sizeof(unsigned long long) * s->brick_cap);
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_stamps, sizeof(int32_t) * s->brick_cap);
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_descs, sizeof(PairDesc) * s->max_admit);
+        if (e == cudaSuccess) e = cudaMemset(s->d_states, 0, sizeof(JobState) * 2 * slots);
+        if (e == cudaSuccess) e = cudaMemset(s->d_ctl, 0, sizeof(Ctl));
+        if (e == cudaSuccess) e = cudaMemset(s->d_stamps, 0, sizeof(int32_t) * s->brick_cap);
+        s->h_pinned_bytes = align_up(sizeof(Ctl)) + align_up(sizeof(JobState) * 2 * slots) +
+                            sizeof(PairDesc) * s->max_admit;
+        if (e == cudaSuccess) e = cudaHostAlloc(&s->h_pinned, s->h_pinned_bytes, cudaHostAllocDefault);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            hd_server_destroy(s);
+            return e == cudaErrorMemoryAllocation ? HD_ERR_OOM : HD_ERR_CUDA;
+        }
+    }
+    s->slots.assign(slots, nullptr);
+    for (int i = slots - 1; i >= 0; --i) s->free_slots.push_back(i);
+    s->worker = std::thread(worker_main, s);
+    *out = s;
+    return HD_OK;
+}
+
+hd_status hd_server_submit(hd_server* s, const hd_pair_desc* pair, uint64_t* ticket) {
+    if (!s || !pair || !ticket || !pair->a || !pair->b) return HD_ERR_BAD_ARG;
+    if ((pair->metric == HD_SE6 ? 0 : 1) != s->se) return HD_ERR_BAD_ARG;
+    if (check_dims(nullptr, pair->W, pair->H, pair->D) != HD_OK) return HD_ERR_BAD_ARG;
+    auto r = std::make_unique<Request>();
+    r->W = pair->W;
+    r->H = pair->H;
+    r->D = pair->D;
+    if (pair->on_device) {
+        r->dev_a = pair->a;
+        r->dev_b = pair->b;
+    } else {
+        const size_t nb = (size_t)pair->W * pair->H * pair->D;
+        r->host_a.assign(pair->a, pair->a + nb);
+        r->host_b.assign(pair->b, pair->b + nb);
+    }
+    plan_request(s, r.get());
+    std::lock_guard<std::mutex> lk(s->mu);
+    if ((int)s->waiting.size() >= s->opt.max_queue) return HD_ERR_BUSY;
+    r->ticket = s->next_ticket++;
+    *ticket = r->ticket;
+    s->waiting.push_back(r.get());
+    s->reqs[r->ticket] = std::move(r);
+    s->stats.submitted += 1;
+    s->cv.notify_all();
+    return HD_OK;
+}
+
+hd_status hd_server_poll(hd_server* s, uint64_t ticket, hd_result* out) {
+    if (!s || !out) return HD_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return HD_ERR_BAD_ARG;
+    if (it->second->state != kDone) return HD_ERR_NOT_READY;
+    *out = it->second->result;
+    s->reqs.erase(it);
+    return HD_OK;
+}
+
+hd_status hd_server_wait(hd_server* s, uint64_t ticket, int64_t timeout_ms, hd_result* out) {
+    if (!s || !out) return HD_ERR_BAD_ARG;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return HD_ERR_BAD_ARG;
+    Request* r = it->second.get();
+    auto ready = [&] { return r->state == kDone; };
+    if (timeout_ms < 0) {
+        s->done_cv.wait(lk, ready);
+    } else if (!s->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
+        return HD_ERR_NOT_READY;
+    }
+    *out = r->result;
+    s->reqs.erase(ticket);
+    return HD_OK;
+}
+
+hd_status hd_server_cancel(hd_server* s, uint64_t ticket) {
+    if (!s) return HD_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return HD_ERR_BAD_ARG;
+    if (it->second->state == kDone) return HD_OK;
+    it->second->cancel = true;
+    s->cv.notify_all();
+    return HD_OK;
+}
+
+hd_status hd_server_get_stats(hd_server* s, hd_server_stats* out) {
+    if (!s || !out) return HD_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->stats;
+    out->waiting_pairs = s->waiting.size();
+    unsigned long long res = 0;
+    for (auto* r : s->slots) res += r != nullptr;
+    out->resident_pairs = res;
+    return HD_OK;
+}
+
+hd_status hd_server_destroy(hd_server* s) {
+    if (!s) return HD_ERR_BAD_ARG;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        s->cv.notify_all();
+    }
+    if (s->worker.joinable()) s->worker.join();
+    {
+        DeviceGuard g(s->ctx->device);
+        if (s->stream) cudaStreamSynchronize(s->stream);
+        for (auto* r : s->slots)
+            if (r && r->resident) cudaFree(r->resident);
+        cudaFree(s->d_jobs);
+        cudaFree(s->d_states);
+        cudaFree(s->d_ctl);
+        for (auto* q : s->d_queue) cudaFree(q);
+        cudaFree(s->d_stamps);
+        cudaFree(s->d_descs);
+        if (s->h_pinned) cudaFreeHost(s->h_pinned);
+        if (s->stream) cudaStreamDestroy(s->stream);
+        cudaGetLastError();
+    }
+    delete s;
+    return HD_OK;
+}
+
+}  // extern "C"

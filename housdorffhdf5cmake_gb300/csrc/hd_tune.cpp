@@ -1,0 +1,185 @@
+// hd_tune.cpp -- autotuner for brick shape and persistent-grid size.
+//
+// Replaces the reference's launch-shape choice by the occupancy API
+// (getOccupancy, hello.cu:1910-1954), whose data-block y size even follows
+// the occupancy result (hello.cu:917).  Here the data layout never depends on
+// the GPU; only the brick shape (words x rows x planes per warp) and the
+// number of resident CTAs per SM are searched, by timing real runs on the
+// caller's pairs.  Winners are kept per workload class and can be persisted
+// as a small JSON table.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "hd/hd.h"
+#include "hd_internal.h"
+
+namespace hdh {
+
+std::string tune_key(int se, double mean_voxels, int npairs) {
+    const int vb = mean_voxels > 1 ? (int)std::lround(std::log2(mean_voxels)) : 0;
+    const char* pc = npairs <= 1 ? "p1" : (npairs < 16 ? "p2" : "p16");
+    char buf[64];
+    std::snprintf(buf, sizeof buf, "se%d/v%d/%s", se == 0 ? 6 : 18, vb, pc);
+    return buf;
+}
+
+bool TuneTable::save(const std::string& path) const {
+    std::ofstream f(path, std::ios::trunc);
+    if (!f) return false;
+    f << "{\n  \"version\": 1,\n  \"entries\": {";
+    bool first = true;
+    for (const auto& kv : entries) {
+        f << (first ? "\n" : ",\n") << "    \"" << kv.first << "\": {\"bxw\": " << kv.second.bxw
+          << ", \"bz\": " << kv.second.bz << ", \"ctas_per_sm\": " << kv.second.ctas_per_sm
+          << ", \"us\": " << kv.second.us << "}";
+        first = false;
+    }
+    f << "\n  }\n}\n";
+    return (bool)f;
+}
+
+// Reads the table written by save(): entries "key": {"bxw": N, "bz": N,
+// "ctas_per_sm": N, "us": X}.  Unknown text is skipped.
+bool TuneTable::load(const std::string& path) {
+    std::ifstream f(path);
+    if (!f) return false;
+    std::stringstream ss;
+    ss << f.rdbuf();
+    const std::string s = ss.str();
+    size_t pos = s.find("\"entries\"");
+    if (pos == std::string::npos) return false;
+    auto field = [](const std::string& body, const char* name, double* v) {
+        const std::string key = std::string("\"") + name + "\"";
+        size_t p = body.find(key);
+        if (p == std::string::npos) return false;
+        p = body.find(':', p);
+        if (p == std::string::npos) return false;
+        *v = std::strtod(body.c_str() + p + 1, nullptr);
+        return true;
+    };
+    while (true) {
+        size_t k0 = s.find('"', pos + 9);
+        if (k0 == std::string::npos) break;
+        size_t k1 = s.find('"', k0 + 1);
+        size_t b0 = s.find('{', k1);
+        size_t b1 = s.find('}', b0);
+        if (k1 == std::string::npos || b0 == std::string::npos || b1 == std::string::npos) break;
+        const std::string key = s.substr(k0 + 1, k1 - k0 - 1);
+        const std::string body = s.substr(b0, b1 - b0 + 1);
+        double bxw = 0, bz = 0, cps = 0, us = 0;
+        if (field(body, "bxw", &bxw) && field(body, "bz", &bz)) {
+            field(body, "ctas_per_sm", &cps);
+            field(body, "us", &us);
+            TuneEntry e;
+            e.bxw = (int)bxw;
+            e.bz = (int)bz;
+            e.ctas_per_sm = (int)cps;
+            e.us = us;
+            entries[key] = e;
+        }
+        pos = b1;
+    }
+    return true;
+}
+
+}  // namespace hdh
+
+using namespace hdh;
+
+extern "C" hd_status hd_autotune(hd_context* ctx, const hd_pair_desc* pairs, int32_t n, int32_t repeats,
+                                 char* report, size_t report_len) {
+    if (!ctx || !pairs || n <= 0) return HD_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    const int se = pairs[0].metric == HD_SE6 ? 0 : 1;
+    for (int i = 0; i < n; ++i) {
+        if (!pairs[i].a || !pairs[i].b || (pairs[i].metric == HD_SE6 ? 0 : 1) != se)
+            return set_error(ctx, HD_ERR_BAD_ARG, "autotune: pairs must share one metric");
+        const hd_status st = check_dims(ctx, pairs[i].W, pairs[i].H, pairs[i].D);
+        if (st != HD_OK) return st;
+    }
+    DeviceGuard g(ctx->device);
+    if (!g.ok) return set_error(ctx, HD_ERR_CUDA, "cannot select device %d", ctx->device);
+    std::vector<PairIn> in;
+    for (int i = 0; i < n; ++i) {
+        PairIn p{pairs[i].a, pairs[i].b, pairs[i].W, pairs[i].H, pairs[i].D, nullptr, nullptr};
+        if (!pairs[i].on_device) {
+            p.a = zero_copy_ptr(ctx, pairs[i].a);
+            p.b = zero_copy_ptr(ctx, pairs[i].b);
+            if (!p.a) p.host_a = pairs[i].a;
+            if (!p.b) p.host_b = pairs[i].b;
+        }
+        in.push_back(p);
+    }
+    repeats = std::max(1, repeats);
+    std::vector<hd_result> res(n), ref(n);
+    const int shapes[][2] = {{2, 4}, {2, 8}, {2, 16}, {4, 4}, {4, 8}, {4, 16}, {8, 4}, {8, 8}, {8, 16}};
+    const int cps_list[] = {0, 1, 2};
+    TuneEntry best;
+    best.us = 1e300;
+    std::string rep;
+    bool have_ref = false;
+    for (const auto& sh : shapes) {
+        for (int cps : cps_list) {
+            RunOpts ro;
+            ro.se = se;
+            ro.bxw = sh[0];
+            ro.bz = sh[1];
+            ro.ctas_per_sm = cps;
+            hd_status st = run_pairs(ctx, in.data(), n, ctx->stream, ro, res.data());  // warm-up
+            if (st != HD_OK && st != HD_EMPTY_MASK) return st;
+            if (!have_ref) {
+                ref = res;
+                have_ref = true;
+            } else {
+                for (int i = 0; i < n; ++i)
+                    if (res[i].hd != ref[i].hd || res[i].sum_ab != ref[i].sum_ab || res[i].sum_ba != ref[i].sum_ba)
+                        return set_error(ctx, HD_ERR_CUDA, "autotune: shape %dx%d gave a different result", sh[0], sh[1]);
+            }
+            std::vector<double> t;
+            for (int r = 0; r < repeats; ++r) {
+                const auto t0 = std::chrono::steady_clock::now();
+                st = run_pairs(ctx, in.data(), n, ctx->stream, ro, res.data());
+                const auto t1 = std::chrono::steady_clock::now();
+                if (st != HD_OK && st != HD_EMPTY_MASK) return st;
+                t.push_back(std::chrono::duration<double, std::micro>(t1 - t0).count());
+            }
+            std::sort(t.begin(), t.end());
+            const double med = t[t.size() / 2];
+            char line[128];
+            std::snprintf(line, sizeof line, "bxw=%d bz=%d cps=%d: %.1f us\n", sh[0], sh[1], cps, med);
+            rep += line;
+            if (med < best.us) {
+                best.us = med;
+                best.bxw = sh[0];
+                best.bz = sh[1];
+                best.ctas_per_sm = cps;
+            }
+        }
+    }
+    double vox = 0;
+    for (const auto& p : in) vox += (double)p.W * p.H * p.D;
+    vox /= n;
+    const std::string key = tune_key(se, vox, n);
+    ctx->tune.entries[key] = best;
+    char line[160];
+    std::snprintf(line, sizeof line, "best %s: bxw=%d bz=%d cps=%d %.1f us\n", key.c_str(), best.bxw, best.bz,
+                  best.ctas_per_sm, best.us);
+    rep += line;
+    if (!ctx->tuning_path.empty() && !ctx->tune.save(ctx->tuning_path))
+        set_error(ctx, HD_OK, "autotune: could not write %s", ctx->tuning_path.c_str());
+    if (report && report_len) {
+        std::strncpy(report, rep.c_str(), report_len - 1);
+        report[report_len - 1] = 0;
+    }
+    return HD_OK;
+}

@@ -1,0 +1,206 @@
+/*
+ * hd.h -- C ABI of the GB300 dilation-based Hausdorff distance library
+ * (libhd_gb300.so).
+ *
+ * This is the drop-in boundary for the reference's single entry point
+ *     int HausdorffDistance::computeDistance(Volume* img1, Volume* img2);
+ * (forBench/HausdorffDistance.cuh:17, implemented at
+ * forBench/HausdorffDistance.cu:101-187).  Plain pointers and sizes only.
+ *
+ * Masks: uint8, nonzero = foreground, x fastest, index x + W*y + W*H*z, the
+ * layout of Volume (forBench/Volume.h:51-54; `bool` is one byte).  Both masks
+ * of a pair share one W x H x D (the reference reads img1's sizes only,
+ * forBench/HausdorffDistance.cu:103).
+ *
+ * Distances are integer dilation counts under a structuring element:
+ *   HD_SE6            6 face neighbours (Manhattan metric)
+ *                     = IS_3D 1, CHEBYSHEV 0 at forBench/HausdorffDistance.cuh:7-8
+ *   HD_SE18_FORBENCH  the reference's shipped default, CHEBYSHEV 1: faces,
+ *                     4 in-plane xy diagonals, 8 corners
+ *                     (forBench/HausdorffDistance.cu:35-58)
+ * hd = min{k : D^k(A) contains B and D^k(B) contains A}, the value the
+ * reference returns.  avg_hd = (sum_ab + sum_ba) / (n_a + n_b) with exact
+ * integer sums of the per-voxel distances (the per-voxel value is the one
+ * hello.cu:1588-1625 records for each newly covered voxel).
+ *
+ * Conventions that differ from the reference on purpose:
+ *   - every call returns an hd_status; nothing exits the process and nothing
+ *     resets the device (the reference exits at :189-195 and calls
+ *     cudaDeviceReset at :181);
+ *   - exactly one empty mask returns HD_EMPTY_MASK at once (the reference
+ *     loops forever); two empty masks give hd = 0;
+ *   - device state belongs to an hd_context; calls on one context are
+ *     serialised by the context's lock; separate contexts run independently.
+ */
+#ifndef HD_HD_H
+#define HD_HD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum hd_status {
+    HD_OK = 0,
+    HD_EMPTY_MASK = 1,       /* exactly one mask is empty: HD undefined */
+    HD_ERR_BAD_ARG = 2,      /* null pointer, non-positive size, unknown metric ... */
+    HD_ERR_OOM = 3,          /* device or pinned-host allocation failed */
+    HD_ERR_CUDA = 4,         /* a CUDA runtime call failed */
+    HD_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+    HD_ERR_CANCELLED = 6,    /* server request cancelled */
+    HD_ERR_ITER_LIMIT = 7,   /* more dilation steps than the volume's diameter */
+    HD_ERR_NOT_READY = 8,    /* server request still in flight */
+    HD_ERR_UNSUPPORTED = 9,  /* feature not compiled in (e.g. HDF5) */
+    HD_ERR_BUSY = 10         /* server admission queue full */
+} hd_status;
+
+typedef enum hd_metric {
+    HD_SE6 = 0,
+    HD_SE18_FORBENCH = 1
+} hd_metric;
+
+/* Per-pair result.  _ab is "A measured against B": sum_ab = sum over a in A
+ * of d(a, B), hd_ab = max over a in A of d(a, B). */
+typedef struct hd_result {
+    int32_t hd;          /* max(hd_ab, hd_ba); -1 when status != HD_OK */
+    int32_t iterations;  /* dilation steps run on the device (max over both directions) */
+    uint64_t sum_ab;
+    uint64_t sum_ba;
+    uint64_t n_a;
+    uint64_t n_b;
+    uint64_t n_a_not_b;
+    uint64_t n_b_not_a;
+    double avg_hd;       /* (sum_ab + sum_ba) / (n_a + n_b); NaN on HD_EMPTY_MASK */
+    int32_t status;      /* hd_status of this pair */
+    int32_t hd_ab;
+    int32_t hd_ba;
+    int32_t hd_robust;   /* percentile HD (hd_options.percentile), stopping rule of hello.cu:1751-1758 */
+} hd_result;
+
+/* Options of a context.  Fill with hd_options_init, then override. */
+typedef struct hd_options {
+    int32_t brick_x_words;       /* brick width in 32-voxel words: 1,2,4,8; 0 = tuned */
+    int32_t brick_z;             /* brick depth in planes: 4, 8, 16; 0 = tuned */
+    int32_t ctas_per_sm;         /* persistent CTAs per SM; 0 = occupancy maximum */
+    int32_t max_iterations;      /* cap on dilation steps; 0 = W + H + D */
+    int64_t barrier_timeout_ns;  /* give-up time of one grid-barrier wait; 0 = 10 s */
+    float percentile;            /* hd_robust percentile in (0, 1]; default 0.95 */
+    int32_t zero_copy;           /* hd_compute_u8: kernels read host masks in place when the
+                                    device can address them (default 1) */
+    const char* tuning_table;    /* autotuner JSON table to load/store; NULL = none */
+} hd_options;
+
+typedef struct hd_context hd_context;
+
+void hd_options_init(hd_options* opt);
+const char* hd_status_string(hd_status s);
+/* Library version string, e.g. "hd_gb300 1.0 sm_103a". */
+const char* hd_version(void);
+
+/* Creates a context on `device` (the reference hard-codes device 0,
+ * forBench/HausdorffDistance.cuh:5).  opt may be NULL. */
+hd_status hd_context_create(int device, const hd_options* opt, hd_context** out);
+hd_status hd_context_destroy(hd_context* ctx);
+/* Text of the last error seen by this context ("" if none). */
+const char* hd_context_last_error(hd_context* ctx);
+
+/* Drop-in for HausdorffDistance::computeDistance (forBench/HausdorffDistance.cu:101):
+ * host masks in, result out.  Host-to-device copies (or zero-copy reads) are
+ * part of the call; the call returns when the result is on the host. */
+hd_status hd_compute_u8(hd_context* ctx, const uint8_t* a, const uint8_t* b, int32_t W, int32_t H,
+                        int32_t D, hd_metric metric, hd_result* out);
+
+/* Same, with the masks already in device memory.  `stream` is a
+ * cudaStream_t (NULL = the context's own stream).  Returns when the result is
+ * on the host. */
+hd_status hd_compute_u8_device(hd_context* ctx, const uint8_t* d_a, const uint8_t* d_b, int32_t W,
+                               int32_t H, int32_t D, hd_metric metric, void* stream,
+                               hd_result* out);
+
+/* One pair of a batch. */
+typedef struct hd_pair_desc {
+    const uint8_t* a;
+    const uint8_t* b;
+    int32_t W, H, D;
+    int32_t metric;      /* hd_metric */
+    int32_t on_device;   /* 1: a and b are device pointers; 0: host pointers */
+    int32_t reserved;
+} hd_pair_desc;
+
+/* Solves n pairs of independent shapes with one packing launch, one set-up
+ * launch and ONE persistent dilation launch over a shared (pair, brick) work
+ * queue.  Per-pair results are bit-identical to hd_compute_u8.  out[i].status
+ * is the status of pair i; the return value is the first hard error. */
+hd_status hd_batch_compute(hd_context* ctx, const hd_pair_desc* pairs, int32_t n, hd_result* out);
+
+/* Instrumented run (not for timing): also returns, per direction, the number
+ * of origin-aligned 32x32x32 tiles that received newly dilated voxels at each
+ * step k (tiles_ab[k]: dilation of B that covers A; tiles_ba[k]: dilation of
+ * A that covers B), k = 0..len-1, and the number of bricks processed. */
+hd_status hd_profile_u8_device(hd_context* ctx, const uint8_t* d_a, const uint8_t* d_b, int32_t W,
+                               int32_t H, int32_t D, hd_metric metric, hd_result* out,
+                               uint64_t* tiles_ab, uint64_t* tiles_ba, int32_t len,
+                               uint64_t* bricks_processed);
+
+/* Per-voxel distances (dense int32, -1 outside the other-mask-complement):
+ * map_a[v] = d(v, B) for v in A \ B, map_b[v] = d(v, A) for v in B \ A, 0 on
+ * A and B overlap, -1 elsewhere.  Device pointers, N = W*H*D int32 each.
+ * Counterpart of the result lists of hello.cu:1588-1625 and the dense map of
+ * hello.cu:2122-2170. */
+hd_status hd_distance_map_device(hd_context* ctx, const uint8_t* d_a, const uint8_t* d_b, int32_t W,
+                                 int32_t H, int32_t D, hd_metric metric, int32_t* d_map_a,
+                                 int32_t* d_map_b, hd_result* out);
+
+/* Autotuner (replaces the occupancy-API launch choice of hello.cu:1910-1954):
+ * times every compiled brick shape and persistent-grid size on the given
+ * pairs (one metric), checks that all give identical results, keeps the
+ * fastest for this workload class in the context and, when the context was
+ * created with hd_options.tuning_table, writes the table there as JSON.  A
+ * human-readable report of the timings goes to `report` (may be NULL). */
+hd_status hd_autotune(hd_context* ctx, const hd_pair_desc* pairs, int32_t n, int32_t repeats,
+                      char* report, size_t report_len);
+
+/* ---- serving: continuous batching under a device-memory budget ---------- */
+typedef struct hd_server hd_server;
+
+typedef struct hd_server_options {
+    uint64_t hbm_budget_bytes;   /* device bytes the server may hold; 0 = 120 GiB */
+    int32_t max_inflight;        /* admitted pairs at once; 0 = unlimited (budget-bound) */
+    int32_t max_queue;           /* waiting requests before submit returns HD_ERR_BUSY; 0 = 4096 */
+    int32_t tick_iterations;     /* dilation steps per device tick; 0 = 16 */
+    int32_t metric;              /* hd_metric of every request of this server */
+} hd_server_options;
+
+void hd_server_options_init(hd_server_options* opt);
+/* Starts a server with its own scheduler thread on ctx's device. */
+hd_status hd_server_create(hd_context* ctx, const hd_server_options* opt, hd_server** out);
+/* Queues a pair (host masks are copied in before submit returns unless
+ * on_device; device masks must stay valid until the request completes). */
+hd_status hd_server_submit(hd_server* srv, const hd_pair_desc* pair, uint64_t* ticket);
+/* HD_ERR_NOT_READY while in flight; otherwise fills *out and forgets the ticket. */
+hd_status hd_server_poll(hd_server* srv, uint64_t ticket, hd_result* out);
+/* Blocks until the request finishes (timeout_ms < 0: no limit). */
+hd_status hd_server_wait(hd_server* srv, uint64_t ticket, int64_t timeout_ms, hd_result* out);
+hd_status hd_server_cancel(hd_server* srv, uint64_t ticket);
+/* Counters: submitted, completed, resident pairs, ticks, device bytes in use. */
+typedef struct hd_server_stats {
+    uint64_t submitted, completed, cancelled, ticks;
+    uint64_t resident_pairs, waiting_pairs;
+    uint64_t bytes_in_use, bytes_peak;
+} hd_server_stats;
+hd_status hd_server_get_stats(hd_server* srv, hd_server_stats* out);
+hd_status hd_server_destroy(hd_server* srv);
+
+/* ---- HDF5 input (forBench/hdf5Manag.cu:44-86, loadHDFIntoBoolArr) -------- */
+/* Reads a rank-1 boolean dataset into a malloc'd byte array.  Returns
+ * HD_ERR_UNSUPPORTED when the library was built without HDF5. */
+hd_status hd_load_hdf5_bool(const char* path, const char* dataset, uint8_t** out, size_t* n);
+void hd_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HD_HD_H */

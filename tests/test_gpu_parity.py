@@ -1,0 +1,269 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
+
+Integer results must be bit-identical: hd, one-sided HDs, the exact distance
+sums and the voxel counts; avg_hd is the same double division of the same
+integers.  The oracle restates forBench/HausdorffDistance.cu:101-187 and is
+itself pinned against breadth-first search and brute force (test_oracle.py).
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from housdorffhdf5cmake_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ("hd", "hd_ab", "hd_ba", "sum_ab", "sum_ba", "n_a", "n_b", "n_a_not_b", "n_b_not_a", "status")
+
+
+def assert_same(g, o, what=""):
+    for k in KEYS:
+        assert g[k] == o[k], f"{what} {k}: gpu {g[k]} oracle {o[k]}\n gpu={g}\n oracle={o}"
+    if o["status"] == 0:
+        assert g["avg_hd"] == o["avg_hd"], what
+    elif o["status"] == 1:
+        assert math.isnan(g["avg_hd"]), what
+
+
+def cuda(x):
+    if isinstance(x, np.ndarray):
+        x = torch.from_numpy(x)
+    return x.to("cuda")
+
+
+def random_pair(rng, shape, p_a=0.01, p_b=0.01, blobs=True):
+    D, H, W = shape
+    a = (rng.random(shape) < p_a).astype(np.uint8)
+    b = (rng.random(shape) < p_b).astype(np.uint8)
+    if blobs and min(shape) >= 4:
+        ta, tb = torch.from_numpy(a), torch.from_numpy(b)
+        for t in (ta, tb):
+            c = [int(rng.integers(0, n)) for n in (W, H, D)]
+            r = [int(rng.integers(1, max(2, n // 3))) for n in (W, H, D)]
+            synth.draw_ellipsoid_into(t, c, r)
+        a, b = ta.numpy(), tb.numpy()
+    return a, b
+
+
+@pytest.mark.parametrize("metric", ["se6", "se18"])
+@pytest.mark.parametrize("seed", [1, 2, 3, 4, 5, 6])
+def test_ellipsoid_salt_64(ctx, oracle, metric, seed):
+    a, b = synth.pair_ellipsoid_salt(seed)
+    a, b = a.numpy(), b.numpy()
+    o = oracle.forbench(a, b, metric)
+    g = ctx.compute(cuda(a), cuda(b), metric)
+    assert_same(g, o, f"seed {seed}")
+    if metric == "se6":
+        bf = oracle.bruteforce_l1(a, b)
+        assert_same(g, bf, f"brute seed {seed}")
+
+
+SHAPES = [
+    (1, 1, 1), (1, 1, 2), (1, 37, 1), (70, 1, 1), (1, 1, 70), (1, 40, 50), (5, 3, 33), (7, 64, 65),
+    (3, 17, 129), (33, 31, 95), (9, 2, 31), (2, 9, 32), (17, 23, 64), (16, 16, 160), (4, 100, 7),
+]
+
+
+@pytest.mark.parametrize("metric", ["se6", "se18"])
+@pytest.mark.parametrize("shape", SHAPES)
+def test_ragged_shapes(ctx, oracle, metric, shape):
+    rng = np.random.default_rng(hash(shape) % (2**32))
+    for trial in range(3):
+        a, b = random_pair(rng, shape, p_a=0.02 * (trial + 1), p_b=0.01, blobs=trial > 0)
+        o = oracle.forbench(a, b, metric)
+        g = ctx.compute(cuda(a), cuda(b), metric)
+        assert_same(g, o, f"{shape} trial {trial}")
+
+
+@pytest.mark.parametrize("metric", ["se6", "se18"])
+def test_edge_cases(ctx, oracle, metric):
+    shape = (20, 30, 70)
+    z = np.zeros(shape, np.uint8)
+    one = z.copy()
+    one[3, 4, 5] = 1
+    far = z.copy()
+    far[-1, -1, -1] = 1
+    full = np.ones(shape, np.uint8)
+    border = z.copy()
+    border[0, :, :] = 1
+    border[:, :, -1] = 1
+    cases = {
+        "both_empty": (z, z),
+        "a_empty": (z, one),
+        "b_empty": (one, z),
+        "identical": (one, one.copy()),
+        "corners": (one, far),
+        "corner_to_corner": (far, np.flip(far).copy()),
+        "full_vs_point": (full, one),
+        "border_planes": (border, far),
+        "full_vs_full": (full, full.copy()),
+    }
+    for name, (a, b) in cases.items():
+        o = oracle.forbench(a, b, metric)
+        g = ctx.compute(cuda(a), cuda(b), metric)
+        assert_same(g, o, name)
+
+
+@pytest.mark.parametrize("metric", ["se6", "se18"])
+def test_brick_shapes_agree(hd, oracle, metric):
+    a, b = synth.pair_shifted_union(11, (48, 96, 160), "cpu", rmin=5, rmax=30, max_shift=8)
+    a, b = a.numpy(), b.numpy()
+    o = oracle.bfs_pair(a, b, metric)
+    da, db = cuda(a), cuda(b)
+    for bxw in (2, 4, 8):
+        for bz in (4, 8, 16):
+            for cps in (0, 1):
+                with hd.Context(0, brick_x_words=bxw, brick_z=bz, ctas_per_sm=cps) as c:
+                    g = c.compute(da, db, metric)
+                assert_same(g, o, f"brick {bxw}x{bz} cps {cps}")
+
+
+def test_shifted_union_midsize(ctx, oracle):
+    for seed in (21, 22):
+        a, b = synth.pair_shifted_union(seed, (96, 160, 192), "cpu", rmin=8, rmax=40, max_shift=12)
+        a, b = a.numpy(), b.numpy()
+        for metric in ("se6", "se18"):
+            o = oracle.bfs_pair(a, b, metric)
+            g = ctx.compute(cuda(a), cuda(b), metric)
+            assert_same(g, o, f"seed {seed} {metric}")
+
+
+def test_host_device_and_zero_copy_paths(hd, ctx, oracle):
+    a, b = synth.pair_shifted_union(5, (40, 72, 100), "cpu", rmin=5, rmax=20, max_shift=6)
+    an, bn = a.numpy(), b.numpy()
+    o = oracle.bfs_pair(an, bn, "se6")
+    assert_same(ctx.compute(an, bn, "se6"), o, "pageable host")
+    assert_same(ctx.compute(a.pin_memory(), b.pin_memory(), "se6"), o, "pinned host")
+    assert_same(ctx.compute(cuda(an), cuda(bn), "se6"), o, "device")
+    with hd.Context(0, zero_copy=False) as c:
+        assert_same(c.compute(an, bn, "se6"), o, "staged copy")
+    # unaligned device pointers take the byte-load packing path
+    big_a = torch.zeros(an.size + 3, dtype=torch.uint8, device="cuda")
+    big_b = torch.zeros(an.size + 5, dtype=torch.uint8, device="cuda")
+    va = big_a[3:].view(an.shape)
+    vb = big_b[5:].view(an.shape)
+    va.copy_(cuda(an))
+    vb.copy_(cuda(bn))
+    assert va.data_ptr() % 16 != 0
+    assert_same(ctx.compute(va, vb, "se6"), o, "unaligned device")
+
+
+def test_batch_equals_plain(ctx, oracle):
+    specs = synth.batch_ragged_specs(3, n=24, lo=16, hi=80, edge_frac=0.2)
+    pairs = [synth.pair_from_spec(s) for s in specs]
+    for metric in ("se6", "se18"):
+        dev = [(cuda(a), cuda(b)) for a, b in pairs]
+        batch = ctx.batch(dev, metric)
+        for i, ((a, b), g) in enumerate(zip(pairs, batch)):
+            plain = ctx.compute(dev[i][0], dev[i][1], metric)
+            assert_same(g, plain, f"pair {i} batch vs plain")
+            o = oracle.forbench(a.numpy(), b.numpy(), metric)
+            assert_same(g, o, f"pair {i} vs oracle ({specs[i].kind})")
+        # host masks in a batch
+        host = ctx.batch([(a.numpy(), b.numpy()) for a, b in pairs[:6]], metric)
+        for i in range(6):
+            assert_same(host[i], batch[i], f"host batch pair {i}")
+
+
+def test_robust_hd(hd, oracle):
+    a, b = synth.pair_shifted_union(8, (40, 80, 96), "cpu", rmin=5, rmax=25, max_shift=10)
+    a, b = a.numpy(), b.numpy()
+    o = oracle.forbench(a, b, "se6", hist=True)
+    for p in (0.5, 0.9, 0.95, 1.0):
+        with hd.Context(0, percentile=p) as c:
+            g = c.compute(cuda(a), cuda(b), "se6")
+        want = oracle.robust_hd(o["hist_ab"], o["hist_ba"], o["n_a_not_b"], o["n_b_not_a"], p)
+        assert g["hd_robust"] == want, p
+    assert g["hd_robust"] == o["hd"]
+
+
+@pytest.mark.parametrize("metric", ["se6", "se18"])
+def test_profile_tile_counts(ctx, oracle, metric):
+    a, b = synth.pair_shifted_union(9, (70, 90, 130), "cpu", rmin=6, rmax=30, max_shift=10)
+    a, b = a.numpy(), b.numpy()
+    g, tab, tba, bricks = ctx.profile(cuda(a), cuda(b), metric)
+    o = oracle.bfs_pair(a, b, metric)
+    assert_same(g, o)
+    D, H, W = a.shape
+    if metric == "se6":
+        zz, yy, xx = np.nonzero(a | b)
+        x0 = (xx.min() // 32) * 32
+        x1 = min(W - 1, (xx.max() // 32) * 32 + 31)
+        box = (x0, x1, yy.min(), yy.max(), zz.min(), zz.max())
+    else:
+        box = (0, W - 1, 0, H - 1, 0, D - 1)
+    da = oracle.bfs_dt(a, metric)
+    db = oracle.bfs_dt(b, metric)
+    want_ba = oracle.tile_counts(da, box, g["hd_ba"])
+    want_ab = oracle.tile_counts(db, box, g["hd_ab"])
+    assert list(tba[: g["hd_ba"] + 1]) == list(want_ba)
+    assert list(tab[: g["hd_ab"] + 1]) == list(want_ab)
+    assert bricks > 0
+
+
+@pytest.mark.parametrize("metric", ["se6", "se18"])
+def test_distance_maps(ctx, oracle, metric):
+    a, b = synth.pair_shifted_union(12, (30, 64, 80), "cpu", rmin=4, rmax=18, max_shift=7)
+    a, b = a.numpy(), b.numpy()
+    g, ma, mb = ctx.distance_map(cuda(a), cuda(b), metric)
+    da = oracle.bfs_dt(a, metric)
+    db = oracle.bfs_dt(b, metric)
+    want_a = np.where(a != 0, np.where(b != 0, 0, db), -1)
+    want_b = np.where(b != 0, np.where(a != 0, 0, da), -1)
+    np.testing.assert_array_equal(ma.cpu().numpy(), want_a)
+    np.testing.assert_array_equal(mb.cpu().numpy(), want_b)
+    assert int(ma.max()) == g["hd_ab"] and int(mb.max()) == g["hd_ba"]
+
+
+def test_determinism(ctx):
+    a, b = synth.pair_shifted_union(4, (64, 128, 128), "cuda", rmin=8, rmax=40, max_shift=12)
+    first = ctx.compute(a, b, "se6")
+    for _ in range(4):
+        assert ctx.compute(a, b, "se6") == first
+
+
+def test_barrier_timeout_returns_status(hd):
+    # A 1 ns give-up time makes the first waiting CTA abandon the grid barrier:
+    # the call must come back with HD_ERR_TIMEOUT and the device stay usable.
+    a, b = synth.pair_shifted_union(2, (32, 64, 64), "cuda", rmin=6, rmax=20, max_shift=8)
+    with hd.Context(0, barrier_timeout_ns=1) as c:
+        with pytest.raises(hd.HDError) as ei:
+            c.compute(a, b, "se6")
+        assert ei.value.code == hd.HD_ERR_TIMEOUT
+    with hd.Context(0) as c:
+        r = c.compute(a, b, "se6")
+        assert r["status"] == 0 and r["hd"] > 0
+
+
+def test_iteration_cap(hd):
+    a = torch.zeros((8, 8, 64), dtype=torch.uint8, device="cuda")
+    b = torch.zeros_like(a)
+    a[0, 0, 0] = 1
+    b[7, 7, 63] = 1
+    with hd.Context(0, max_iterations=5) as c:
+        with pytest.raises(hd.HDError) as ei:
+            c.compute(a, b, "se6")
+        assert ei.value.code == hd.HD_ERR_ITER_LIMIT
+
+
+def test_bad_arguments(hd, ctx):
+    a = torch.zeros((4, 4, 4), dtype=torch.uint8, device="cuda")
+    with pytest.raises(ValueError):
+        ctx.compute(a, torch.zeros((4, 4, 5), dtype=torch.uint8, device="cuda"))
+    with pytest.raises(ValueError):
+        ctx.compute(a, a, metric="se26")
+
+
+def test_reference_class_mirror(hd, oracle):
+    a, b = synth.pair_ellipsoid_salt(7)
+    a, b = a.numpy(), b.numpy()
+    v1, v2 = hd.Volume.from_array(a), hd.Volume.from_array(b)
+    h = hd.HausdorffDistance()  # reference default: 18-neighbour element
+    assert h.computeDistance(v1, v2) == oracle.forbench(a, b, "se18")["hd"]
+    d, avg = hd.HausdorffDistance("se6").computeDistances(v1, v2)
+    o = oracle.forbench(a, b, "se6")
+    assert d == o["hd"] and avg == o["avg_hd"]
+    empty = hd.Volume(64, 64, 64)
+    assert h.computeDistance(v1, empty) == -1
