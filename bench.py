@@ -1,0 +1,421 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 dilation-based Hausdorff distance.
+
+Headline workload (one step = one pair): two 512x512x256 uint8 CT-like masks
+(union of 1-4 ellipsoids, second mask shifted by up to +-15 voxels with 0.5%
+boundary flips), 6-neighbour element, packed 32 voxels per uint32 along x.
+The reference's own data (512x512x826 lung/bladder HDF5 masks) is not
+available; the masks are seeded synthetic stand-ins with the stated shapes.
+
+  value  pairs/s with the masks resident in HBM (hd_compute_u8_device), CUDA
+         events on the launch stream, L2 flushed (256 MiB write) between steps
+         outside the timed events
+  e2e    pairs/s through hd_compute_u8 with pinned HOST masks: the device
+         reads the masks over the host link inside the call, results come back
+         to the host
+Extra keys: Gvoxel-iter/s, the roofline of the dominant kernel, the serial
+CPU baseline (the oracle's restatement of the reference loop, 1 core), the
+ragged 256-pair batch (one persistent launch) against the same pairs one call
+each, and the 512^3 far-blob worst case of the frontier queue.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun every rank computes its own pair (replicas, weak scaling) and
+rank 0 prints one JSON line.  --impl reference times the reference algorithm
+on the host cores (the oracle's restatement of forBench/HausdorffDistance.cu
+with all host threads) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W_, H_, D_ = 512, 512, 256
+WORKLOAD = "plain single pair 512x512x256 uint8, 6-neighbour element (CT-like shifted ellipsoid unions)"
+
+
+def _dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    parts = [p.strip() for p in line.split(",")]
+                    if len(parts) >= 9:
+                        rows.append(parts)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def _flush_l2(buf):
+    buf.zero_()
+
+
+def bench_ours(args):
+    import numpy as np
+    import torch
+
+    import housdorffhdf5cmake_gb300 as hd
+    from housdorffhdf5cmake_gb300 import synth
+
+    ws, rank, local = _dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    seed = 1234 + rank
+    a, b = synth.pair_shifted_union(seed, (D_, H_, W_), dev)
+    N = W_ * H_ * D_
+    ctx = hd.Context(local, record_timings=True)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+
+    ref = ctx.compute(a, b, "se6")
+    for _ in range(args.warmup):
+        r = ctx.compute(a, b, "se6")
+        assert r == ref, "non-deterministic result"
+
+    # ---- device-resident timed region ---------------------------------------
+    times, phases = [], []
+    clocks = ClockSampler(local)
+    with clocks:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            _flush_l2(flush)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r = ctx.compute(a, b, "se6")
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            phases.append(ctx.last_timings())
+            assert r == ref
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        wall = time.perf_counter() - wall0
+    clk = clocks.summary()
+    step_ms = sum(times) / len(times)
+    if dist:
+        t = torch.tensor([step_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = ws * 1000.0 / step_ms
+
+    # ---- end to end through the host API (pinned host masks) ----------------
+    ha, hb = a.cpu().pin_memory(), b.cpu().pin_memory()
+    for _ in range(max(1, args.warmup)):
+        assert ctx.compute(ha, hb, "se6") == ref
+    e2e_t = []
+    if dist:
+        dist.barrier()
+    for _ in range(args.steps):
+        _flush_l2(flush)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = ctx.compute(ha, hb, "se6")
+        e2e_t.append((time.perf_counter() - t0) * 1000.0)
+        assert r == ref
+    e2e_ms = sum(e2e_t) / len(e2e_t)
+    if dist:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    kmax = W_ + H_ + D_
+    d2h = 768 + 2 * 8 * (kmax + 1)
+
+    # ---- roofline of the dominant kernel -------------------------------------
+    res, tab, tba, bricks = ctx.profile(a, b, "se6")
+    tiles = int(sum(int(x) for x in tab[1: res["hd_ab"] + 1]) + sum(int(x) for x in tba[1: res["hd_ba"] + 1]))
+    b_iter = 3 * 4096 * tiles
+    b_pack = 2 * N + 2 * (N // 8)
+    pk = statistics.mean(p["pack_ms"] for p in phases)
+    su = statistics.mean(p["setup_ms"] for p in phases)
+    so = statistics.mean(p["solve_ms"] for p in phases)
+    peak, peak_kind = _peaks()
+    share = {"pack": pk, "setup": su, "solve": so}
+    dom = max(share, key=share.get)
+    if dom == "solve":
+        achieved = b_iter / (so * 1e-3) / 1e9
+        alg = b_iter
+    elif dom == "pack":
+        achieved = b_pack / (pk * 1e-3) / 1e9
+        alg = b_pack
+    else:
+        achieved = None
+        alg = None
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            traffic = json.load(f).get("c2_512x512x256_se6", {}).get(dom)
+    except Exception:
+        traffic = None
+    roofline = {
+        "bound": "hbm", "kernel": {"solve": "solve_kernel (persistent frontier dilation)", "pack": "pack_kernel",
+                                   "setup": "setup_kernel"}[dom],
+        "achieved": round(achieved, 1) if achieved else None, "peak": peak, "unit": "GB/s",
+        "frac": round(achieved / peak, 4) if achieved else None, "peak_source": f"{peak_kind} MEASURED_PEAKS hbm_gbs",
+        "traffic": traffic, "algorithmic_bytes": alg,
+        "phase_ms": {k: round(v, 4) for k, v in share.items()},
+        "pack": {"bytes": b_pack, "ms": round(pk, 4), "gbs": round(b_pack / (pk * 1e-3) / 1e9, 1)},
+        "solve": {"bytes": b_iter, "ms": round(so, 4), "gbs": round(b_iter / (so * 1e-3) / 1e9, 1),
+                  "frontier_tiles": tiles, "bricks_processed": bricks},
+    }
+    gvox = ref["hd"] * 2 * N / (step_ms * 1e-3) / 1e9
+
+    out = {
+        "metric": "mask-pairs/sec", "value": round(value, 3), "unit": "pairs/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32 (bit-packed binary masks, integer dilation counts)",
+        "data": "synthetic seeded masks (reference data not available)",
+        "config": {"workload": WORKLOAD, "W": W_, "H": H_, "D": D_, "element": "se6",
+                   "l2": "flushed between steps (256 MiB write, outside the timed events)",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                   "brick": [phases[-1]["brick_x_words"], 32 // max(1, phases[-1]["brick_x_words"]),
+                             phases[-1]["brick_z"]], "grid_ctas": phases[-1]["grid_ctas"]},
+        "hd": ref["hd"], "avg_hd": ref["avg_hd"], "iterations": phases[-1]["iterations"],
+        "gvoxel_iter_per_s": round(gvox, 2),
+        "e2e": {"value": round(ws * 1000.0 / e2e_ms, 3), "unit": "pairs/s", "ms_per_step": round(e2e_ms, 4),
+                "h2d_bytes_per_step": 2 * N, "d2h_bytes_per_step": d2h,
+                "path": "hd_compute_u8, pinned host masks read by the packing kernel over the host link"},
+        "gpu_launches": 3 * args.steps,
+        "roofline": roofline, "clocks": clk, "wall_s_timed_region": round(wall, 3),
+    }
+
+    if rank == 0 and ws == 1 and not args.no_extras:
+        out["batched"] = bench_batched(ctx, args)
+        out["worst_case"] = bench_worst_case(ctx, dev)
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(a.cpu().numpy(), b.cpu().numpy(), ref)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def bench_batched(ctx, args):
+    """256 ragged pairs: one persistent launch vs one call per pair."""
+    import torch
+
+    from housdorffhdf5cmake_gb300 import synth
+    specs = synth.batch_ragged_specs(77, n=256)
+    pairs = [synth.pair_from_spec(s, "cuda") for s in specs]
+    voxels = sum(s.shape[0] * s.shape[1] * s.shape[2] for s in specs)
+    batch = ctx.batch(pairs, "se6")
+    plain = [ctx.compute(a, b, "se6") for a, b in pairs]
+    # every result field except `iterations` (the shared loop's length in a batch)
+    keys = ("hd", "hd_ab", "hd_ba", "hd_robust", "sum_ab", "sum_ba", "n_a", "n_b", "n_a_not_b", "n_b_not_a",
+            "status")
+    exact = all(x[k] == y[k] for x, y in zip(batch, plain) for k in keys)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, reps):
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    reps = max(2, min(args.steps, 3))
+    t_batch = timed(lambda: ctx.batch(pairs, "se6"), reps)
+    t_plain = timed(lambda: [ctx.compute(a, b, "se6") for a, b in pairs], reps)
+    gvox = sum(max(0, r["hd"]) * 2 * (s.shape[0] * s.shape[1] * s.shape[2]) for r, s in zip(batch, specs))
+    return {
+        "workload": "256 ragged pairs, axes uniform in {64..384}, 5% edge pairs (empty / identical)",
+        "pairs": len(pairs), "voxels": voxels,
+        "batched_pairs_per_s": round(256 * 1000.0 / t_batch, 2), "batched_ms": round(t_batch, 3),
+        "plain_pairs_per_s": round(256 * 1000.0 / t_plain, 2), "plain_ms": round(t_plain, 3),
+        "speedup_batched_vs_plain": round(t_plain / t_batch, 2),
+        "gvoxel_iter_per_s_batched": round(gvox / (t_batch * 1e-3) / 1e9, 2),
+        "bit_exact_vs_plain": bool(exact),
+    }
+
+
+def bench_worst_case(ctx, dev):
+    """512^3, 8 small blobs vs 8 blobs >= 200 voxels away: long sparse frontier."""
+    import torch
+
+    from housdorffhdf5cmake_gb300 import synth
+    a, b = synth.pair_far_blobs(5, (512, 512, 512), dev)
+    ctx.compute(a, b, "se6")
+    stream = torch.cuda.current_stream()
+    ts = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = ctx.compute(a, b, "se6")
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    t = statistics.median(ts)
+    tim = ctx.last_timings()
+    res, tab, tba, bricks = ctx.profile(a, b, "se6")
+    nz = torch.nonzero(a | b)
+    lo, hi = nz.min(0).values.tolist(), nz.max(0).values.tolist()  # (z, y, x)
+    bxw, bz = tim["brick_x_words"], tim["brick_z"]
+    by = 32 // bxw
+    wx = (hi[2] // 32) - (lo[2] // 32) + 1
+    dom_bricks = -(-wx // bxw) * -(-(hi[1] - lo[1] + 1) // by) * -(-(hi[0] - lo[0] + 1) // bz)
+    iters = max(1, res["hd_ab"]) + max(1, res["hd_ba"])
+    N = 512 ** 3
+    return {
+        "workload": "512^3, 8 balls r 3-6 vs 8 balls >= 200 voxels away, 6-neighbour element",
+        "hd": r["hd"], "iterations": tim["iterations"], "ms": round(t, 3),
+        "ms_per_iteration": round(t / max(1, tim["iterations"]), 4),
+        "pairs_per_s": round(1000.0 / t, 3),
+        "gvoxel_iter_per_s": round(r["hd"] * 2 * N / (t * 1e-3) / 1e9, 2),
+        "active_brick_fraction_mean": round(bricks / (dom_bricks * iters), 4),
+        "solve_ms": round(tim["solve_ms"], 3), "pack_ms": round(tim["pack_ms"], 3),
+    }
+
+
+def cpu_baseline(a_np, b_np, ref):
+    """Serial restatement of the reference loop on the host (1 core)."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    o = O.forbench(a_np, b_np, "se6", nthreads=1)
+    dt = time.perf_counter() - t0
+    assert o["hd"] == ref["hd"] and o["sum_ab"] == ref["sum_ab"] and o["sum_ba"] == ref["sum_ba"]
+    return {"value": round(1.0 / dt, 5), "unit": "pairs/s", "cores": 1, "kind": "port",
+            "sample": f"the full headline pair ({W_}x{H_}x{D_}), one run, {dt:.1f} s, "
+                      "oracle restatement of forBench/HausdorffDistance.cu:101-187 (serial scatter form)",
+            "seconds": round(dt, 3)}
+
+
+def bench_reference(args):
+    """The reference algorithm on the host cores (oracle port, all threads)."""
+    ws, rank, local = _dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+
+    from housdorffhdf5cmake_gb300 import synth
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    a, b = synth.pair_shifted_union(1234, (D_, H_, W_), "cpu")
+    a, b = a.numpy(), b.numpy()
+    for _ in range(args.warmup):
+        O.forbench(a, b, "se6", nthreads=threads)
+    ts = []
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o = O.forbench(a, b, "se6", nthreads=threads)
+        ts.append(time.perf_counter() - t0)
+    t_all = time.perf_counter() - t_all
+    step = sum(ts) / len(ts)
+    v = 1.0 / step
+    out = {
+        "impl": "reference", "metric": "mask-pairs/sec", "value": round(v, 5), "unit": "pairs/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step * 1000, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8 (byte per voxel)",
+        "data": "synthetic seeded masks (reference data not available)",
+        "config": {"workload": WORKLOAD, "W": W_, "H": H_, "D": D_, "element": "se6"},
+        "hd": o["hd"],
+        "cpu_baseline": {"value": round(v, 5), "unit": "pairs/s", "cores": threads, "kind": "port",
+                         "sample": "the full headline pair per step: oracle restatement of "
+                                   "forBench/HausdorffDistance.cu:101-187, OpenMP gather form, all host threads"},
+        "e2e": {"value": round(v, 5), "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched and worst-case sub-results")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        bench_reference(args)
+    else:
+        bench_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -109,7 +109,8 @@ class Context:
     """
 
     def __init__(self, device: int = 0, *, brick_x_words=0, brick_z=0, ctas_per_sm=0, max_iterations=0,
-                 barrier_timeout_ns=0, percentile=0.95, zero_copy=True, tuning_table=None):
+                 barrier_timeout_ns=0, percentile=0.95, zero_copy=True, tuning_table=None,
+                 record_timings=False):
         L = N.load()
         opt = N.HdOptions()
         L.hd_options_init(ctypes.byref(opt))
@@ -122,6 +123,7 @@ class Context:
         opt.zero_copy = 1 if zero_copy else 0
         self._tuning = tuning_table.encode() if tuning_table else None
         opt.tuning_table = self._tuning
+        opt.record_timings = 1 if record_timings else 0
         h = ctypes.c_void_p()
         code = L.hd_context_create(int(device), ctypes.byref(opt), ctypes.byref(h))
         if code != HD_OK:
@@ -153,6 +155,12 @@ class Context:
 
     def last_error(self) -> str:
         return (N.load().hd_context_last_error(self._h) or b"").decode()
+
+    def last_timings(self) -> dict:
+        """Kernel durations of the last pair computation (record_timings=True)."""
+        t = N.HdTimings()
+        N.load().hd_context_last_timings(self._h, ctypes.byref(t))
+        return t.as_dict()
 
     # -- single pair --------------------------------------------------------
     def compute(self, a, b, metric="se6", stream=None) -> dict:

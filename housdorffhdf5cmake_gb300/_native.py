@@ -29,7 +29,7 @@ HD_SE18_FORBENCH = 1
 # Every entry point of include/hd/hd.h.
 EXPORTS = (
     "hd_options_init", "hd_status_string", "hd_version", "hd_context_create", "hd_context_destroy",
-    "hd_context_last_error", "hd_compute_u8", "hd_compute_u8_device", "hd_batch_compute",
+    "hd_context_last_error", "hd_context_last_timings", "hd_compute_u8", "hd_compute_u8_device", "hd_batch_compute",
     "hd_profile_u8_device", "hd_distance_map_device", "hd_autotune", "hd_server_options_init",
     "hd_server_create", "hd_server_submit", "hd_server_poll", "hd_server_wait", "hd_server_cancel",
     "hd_server_get_stats", "hd_server_destroy", "hd_load_hdf5_bool", "hd_free",
@@ -67,7 +67,24 @@ class HdOptions(ctypes.Structure):
         ("percentile", ctypes.c_float),
         ("zero_copy", ctypes.c_int32),
         ("tuning_table", ctypes.c_char_p),
+        ("record_timings", ctypes.c_int32),
     ]
+
+
+class HdTimings(ctypes.Structure):
+    _fields_ = [
+        ("pack_ms", ctypes.c_float),
+        ("setup_ms", ctypes.c_float),
+        ("solve_ms", ctypes.c_float),
+        ("total_ms", ctypes.c_float),
+        ("iterations", ctypes.c_int32),
+        ("grid_ctas", ctypes.c_int32),
+        ("brick_x_words", ctypes.c_int32),
+        ("brick_z", ctypes.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class HdPairDesc(ctypes.Structure):
@@ -140,6 +157,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             "hd_context_create": (st, [ctypes.c_int, ctypes.POINTER(HdOptions), ctypes.POINTER(vp)]),
             "hd_context_destroy": (st, [vp]),
             "hd_context_last_error": (ctypes.c_char_p, [vp]),
+            "hd_context_last_timings": (st, [vp, ctypes.POINTER(HdTimings)]),
             "hd_compute_u8": (st, [vp, vp, vp, i32, i32, i32, st, res_p]),
             "hd_compute_u8_device": (st, [vp, vp, vp, i32, i32, i32, st, vp, res_p]),
             "hd_batch_compute": (st, [vp, ctypes.POINTER(HdPairDesc), i32, res_p]),

@@ -392,6 +392,8 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     for (int i = 0; i < n; ++i) max_words = std::max(max_words, plan[i].full_words);
     const int grid_x = (int)std::min<long long>(1024, std::max<long long>(1, (max_words + 2047) / 2048));
     const PairDesc* ddesc = (const PairDesc*)(dbase + off_descs);
+    const bool timing = ctx->opt.record_timings != 0 && ctx->ev[0] != nullptr;
+    if (timing) cudaEventRecord(ctx->ev[0], s);
     e = hdk::launch_pack(ddesc, n, grid_x, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "pack launch");
     Ctl* dctl = (Ctl*)(dbase + off_ctl);
@@ -400,6 +402,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     unsigned long long* dq[3] = {(unsigned long long*)(dbase + off_q[0]),
                                  (unsigned long long*)(dbase + off_q[1]),
                                  (unsigned long long*)(dbase + off_q[2])};
+    if (timing) cudaEventRecord(ctx->ev[1], s);
     e = hdk::launch_setup(ddesc, n, grid_x, djobs, dstates, dq[g0 % 3], dctl, g0, bxw, bz, stats ? 1 : 0, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "setup launch");
     if (ro.map_a || ro.map_b) {
@@ -428,8 +431,10 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     const int per_sm = cps > 0 ? std::min(cps, occ) : occ;
     dim3 grid(ctx->sm_count * per_sm), block(256);
     void* args[] = {&sp};
+    if (timing) cudaEventRecord(ctx->ev[2], s);
     e = cudaLaunchCooperativeKernel(solve_fn, grid, block, args, 0, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "dilation launch");
+    if (timing) cudaEventRecord(ctx->ev[3], s);
 
     // ---- read-back ------------------------------------------------------------
     e = cudaMemcpyAsync(hbase, dbase, readback_bytes, cudaMemcpyDeviceToHost, s);
@@ -456,6 +461,17 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     const PairInfo* hin = (const PairInfo*)(hbase + off_infos);
     const uint64_t* hh = (const uint64_t*)(hbase + upload_bytes);
     ctx->g_next = std::max(ctx->g_next, hctl->g_end) + 2;
+    if (timing) {
+        hd_timings& T = ctx->last_timings;
+        cudaEventElapsedTime(&T.pack_ms, ctx->ev[0], ctx->ev[1]);
+        cudaEventElapsedTime(&T.setup_ms, ctx->ev[1], ctx->ev[2]);
+        cudaEventElapsedTime(&T.solve_ms, ctx->ev[2], ctx->ev[3]);
+        cudaEventElapsedTime(&T.total_ms, ctx->ev[0], ctx->ev[3]);
+        T.iterations = hctl->iters_run;
+        T.grid_ctas = (int)grid.x;
+        T.brick_x_words = bxw;
+        T.brick_z = bz;
+    }
     const float pct = (ctx->opt.percentile > 0.f && ctx->opt.percentile <= 1.f) ? ctx->opt.percentile : 0.95f;
     hd_status first = HD_OK;
     size_t hoff = 0, toff = 0;
@@ -564,6 +580,8 @@ hd_status hd_context_create(int device, const hd_options* opt, hd_context** out)
             return HD_ERR_CUDA;
         }
         ctx->pageable_ats = ats;
+        if (ctx->opt.record_timings)
+            for (auto& ev : ctx->ev) cudaEventCreate(&ev);
     }
     if (!ctx->tuning_path.empty()) ctx->tune.load(ctx->tuning_path);
     *out = ctx;
@@ -579,6 +597,8 @@ hd_status hd_context_destroy(hd_context* ctx) {
         ctx->arena.release();
         ctx->stamps.release();
         ctx->pinned.release();
+        for (auto& ev : ctx->ev)
+            if (ev) cudaEventDestroy(ev);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
         ctx->stream = nullptr;
     }
@@ -587,6 +607,13 @@ hd_status hd_context_destroy(hd_context* ctx) {
 }
 
 const char* hd_context_last_error(hd_context* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+hd_status hd_context_last_timings(hd_context* ctx, hd_timings* out) {
+    if (!ctx || !out) return HD_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    *out = ctx->last_timings;
+    return HD_OK;
+}
 
 static hd_status metric_to_se(hd_context* ctx, int metric, int* se) {
     if (metric == HD_SE6) *se = 0;

@@ -72,6 +72,8 @@ struct hd_context {
     hdh::PinnedArena pinned;
     std::map<const void*, int> occupancy;  // persistent kernel -> resident CTAs per SM
     hdh::TuneTable tune;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // record_timings: before pack/setup/solve, after solve
+    hd_timings last_timings{};
 };
 
 namespace hdh {

@@ -90,7 +90,20 @@ typedef struct hd_options {
     int32_t zero_copy;           /* hd_compute_u8: kernels read host masks in place when the
                                     device can address them (default 1) */
     const char* tuning_table;    /* autotuner JSON table to load/store; NULL = none */
+    int32_t record_timings;      /* record CUDA events around each kernel (hd_context_last_timings) */
 } hd_options;
+
+/* Device durations of the last call's kernels (record_timings = 1), measured
+ * with CUDA events on the stream the kernels were launched on. */
+typedef struct hd_timings {
+    float pack_ms;       /* bit packing + bounding box + counts */
+    float setup_ms;      /* crop into job domains + first-step queue */
+    float solve_ms;      /* persistent dilation loop */
+    float total_ms;      /* first launch to last kernel end */
+    int32_t iterations;  /* dilation steps run by the persistent loop */
+    int32_t grid_ctas;   /* CTAs of the persistent launch */
+    int32_t brick_x_words, brick_z;
+} hd_timings;
 
 typedef struct hd_context hd_context;
 
@@ -105,6 +118,9 @@ hd_status hd_context_create(int device, const hd_options* opt, hd_context** out)
 hd_status hd_context_destroy(hd_context* ctx);
 /* Text of the last error seen by this context ("" if none). */
 const char* hd_context_last_error(hd_context* ctx);
+/* Kernel timings of the context's last pair computation (zeros unless the
+ * context was created with record_timings = 1). */
+hd_status hd_context_last_timings(hd_context* ctx, hd_timings* out);
 
 /* Drop-in for HausdorffDistance::computeDistance (forBench/HausdorffDistance.cu:101):
  * host masks in, result out.  Host-to-device copies (or zero-copy reads) are

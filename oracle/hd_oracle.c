@@ -88,10 +88,9 @@ static void finish_avg(or_result* r) {
  *   neighbours of the Write buffer (:24-91), the cover test of :96 is ANDed
  *   over all voxels, then Write is copied to Read (:161-162) and the loop
  *   counter is incremented (:171).
- * nthreads > 1: the same iteration as a gather (Write[v] = Read[v] or any
- *   in-volume neighbour of v set in Read).  The elements are symmetric, so the
- *   gather and the scatter set exactly the same voxels; the z-planes are split
- *   across OpenMP threads without write races.
+ * nthreads > 1: the same scatter and copy with the z-planes split across
+ *   OpenMP threads (stores into another thread's planes are relaxed atomic
+ *   byte stores of the same value 1).
  *
  * The reference loops forever when exactly one mask is empty (the test at :96
  * can never become true); here that case returns OR_EMPTY at once.  Each loop
@@ -194,23 +193,31 @@ int or_forbench(const uint8_t* A, const uint8_t* B, int W, int H, int D, int se,
             if (new_b) hd_ba = j;
             if (hist_ab && j < hist_len) hist_ab[j] += new_a;
             if (hist_ba && j < hist_len) hist_ba[j] += new_b;
+            /* dilate: the scatter of :24-91 split over z-planes; writes that
+             * cross into a neighbouring thread's planes are relaxed atomic
+             * byte stores of 1 (all writers store the same value). */
 #pragma omp parallel for schedule(static)
             for (int z = 0; z < D; ++z)
                 for (int y = 0; y < H; ++y)
                     for (int x = 0; x < W; ++x) {
                         const size_t id = (size_t)z * WH + (size_t)y * W + x;
-                        int g1 = r1[id], g2 = r2[id];
-                        for (int s = 0; s < nse && !(g1 && g2); ++s) {
-                            const int nx = x - SE_OFFS[s][0], ny = y - SE_OFFS[s][1],
-                                      nz = z - SE_OFFS[s][2];
+                        const int s1 = r1[id], s2 = r2[id];
+                        if (!s1 && !s2) continue;
+                        for (int s = 0; s < nse; ++s) {
+                            const int nx = x + SE_OFFS[s][0], ny = y + SE_OFFS[s][1],
+                                      nz = z + SE_OFFS[s][2];
                             if (nx < 0 || nx >= W || ny < 0 || ny >= H || nz < 0 || nz >= D) continue;
                             const size_t nid = (size_t)nz * WH + (size_t)ny * W + nx;
-                            g1 |= r1[nid]; g2 |= r2[nid];
+                            if (s1) __atomic_store_n(&w1[nid], (uint8_t)1, __ATOMIC_RELAXED);
+                            if (s2) __atomic_store_n(&w2[nid], (uint8_t)1, __ATOMIC_RELAXED);
                         }
-                        w1[id] = (uint8_t)g1; w2[id] = (uint8_t)g2;
                     }
-            uint8_t* t = r1; r1 = w1; w1 = t;
-            t = r2; r2 = w2; w2 = t;
+            /* Write -> Read */
+#pragma omp parallel for schedule(static)
+            for (int z = 0; z < D; ++z) {
+                memcpy(r1 + (size_t)z * WH, w1 + (size_t)z * WH, WH);
+                memcpy(r2 + (size_t)z * WH, w2 + (size_t)z * WH, WH);
+            }
             ++distance;
             if (distance > max_trips) { status = OR_ITER; break; }
         }

@@ -1,0 +1,99 @@
+"""Serving loop: continuous batching.  Every result must be bit-identical to
+the single-pair path, whether the pair runs alone or in a mix that joins the
+device loop at different ticks."""
+import time
+
+import numpy as np
+import pytest
+import torch
+
+from housdorffhdf5cmake_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ("hd", "hd_ab", "hd_ba", "hd_robust", "sum_ab", "sum_ba", "n_a", "n_b", "n_a_not_b", "n_b_not_a", "status")
+
+
+def same(x, y):
+    return all(x[k] == y[k] for k in KEYS)
+
+
+def _pairs(n, seed, lo=24, hi=96, edge=0.15):
+    specs = synth.batch_ragged_specs(seed, n=n, lo=lo, hi=hi, edge_frac=edge)
+    return [synth.pair_from_spec(s, "cuda") for s in specs]
+
+
+def test_server_matches_plain_path(hd, ctx):
+    pairs = _pairs(40, 5)
+    plain = [ctx.compute(a, b, "se6") for a, b in pairs]
+    with hd.Server(ctx, tick_iterations=4) as srv:
+        tickets = []
+        for i, (a, b) in enumerate(pairs):
+            tickets.append(srv.submit(a, b))
+            if i % 7 == 0:
+                time.sleep(0.002)  # later arrivals join a loop already in flight
+        res = [srv.wait(t, 60000) for t in tickets]
+        st = srv.stats()
+    for i, (r, p) in enumerate(zip(res, plain)):
+        assert same(r, p), (i, r, p)
+    assert st["completed"] == len(pairs) and st["ticks"] > 1
+
+
+def test_alone_equals_in_mix(hd, ctx):
+    pairs = _pairs(12, 9, lo=32, hi=128, edge=0.0)
+    probe = pairs[3]
+    with hd.Server(ctx) as srv:
+        alone = srv.wait(srv.submit(*probe), 60000)
+    with hd.Server(ctx, tick_iterations=2) as srv:
+        ts = [srv.submit(a, b) for a, b in pairs[:3]]
+        time.sleep(0.005)
+        tp = srv.submit(*probe)
+        ts += [srv.submit(a, b) for a, b in pairs[4:]]
+        mixed = srv.wait(tp, 60000)
+        for t in ts:
+            srv.wait(t, 60000)
+    assert same(alone, mixed)
+
+
+def test_host_masks_and_se18(hd, ctx):
+    pairs = _pairs(10, 11)
+    host = [(a.cpu().numpy(), b.cpu().numpy()) for a, b in pairs]
+    with hd.Server(ctx, metric="se18") as srv:
+        ts = [srv.submit(a, b) for a, b in host]
+        res = [srv.wait(t, 60000) for t in ts]
+    for (a, b), r in zip(pairs, res):
+        assert same(r, ctx.compute(a, b, "se18"))
+
+
+def test_budget_admission_and_oversize(hd, ctx):
+    pairs = _pairs(16, 13, lo=64, hi=96, edge=0.0)
+    budget = 24 << 20  # a few pairs at a time
+    with hd.Server(ctx, hbm_budget_bytes=budget) as srv:
+        big = torch.zeros((256, 256, 256), dtype=torch.uint8, device="cuda")
+        tbig = srv.submit(big, big)
+        ts = [srv.submit(a, b) for a, b in pairs]
+        res = [srv.wait(t, 60000) for t in ts]
+        rbig = srv.wait(tbig, 60000)
+        st = srv.stats()
+    assert rbig["status"] == hd.HD_ERR_OOM
+    assert st["bytes_peak"] <= budget
+    for (a, b), r in zip(pairs, res):
+        assert same(r, ctx.compute(a, b, "se6"))
+
+
+def test_cancel(hd, ctx):
+    pairs = _pairs(30, 17, lo=96, hi=160, edge=0.0)
+    with hd.Server(ctx, tick_iterations=1, max_inflight=4) as srv:
+        ts = [srv.submit(a, b) for a, b in pairs]
+        for t in ts[::3]:
+            srv.cancel(t)
+        res = [srv.wait(t, 60000) for t in ts]
+        st = srv.stats()
+    for i, ((a, b), r) in enumerate(zip(pairs, res)):
+        if i % 3 == 0:
+            assert r["status"] in (hd.HD_ERR_CANCELLED, hd.HD_OK)
+            if r["status"] == hd.HD_OK:
+                assert same(r, ctx.compute(a, b, "se6"))
+        else:
+            assert same(r, ctx.compute(a, b, "se6"))
+    assert st["cancelled"] >= 1
