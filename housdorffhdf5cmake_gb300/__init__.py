@@ -287,7 +287,12 @@ class Server:
         self._keep = {}
 
     def submit(self, a, b) -> int:
+        """Queue a pair.  CUDA masks are read later on the server's own
+        stream, so the work that produced them is waited for here."""
         A, B = _Buf(a), _Buf(b)
+        if A.on_device or B.on_device:
+            import torch
+            torch.cuda.current_stream().synchronize()
         d = N.HdPairDesc()
         d.a, d.b = A.ptr, B.ptr
         d.W, d.H, d.D = A.W, A.H, A.D

@@ -47,6 +47,8 @@ struct PairDesc {
     PairInfo* info;
     int32_t* tstamp[2];            // instrumented runs only (else null)
     unsigned long long* tcount[2];
+    uint32_t epoch;                // queue-entry tag of this pair's jobs (slot reuse)
+    uint32_t pad_;
 };
 
 // One direction of a pair, written by the set-up kernel.
@@ -65,7 +67,14 @@ struct Job {
     unsigned long long brick0;
     int32_t* tstamp;           // instrumented runs: per full-volume tile, last marked step
     unsigned long long* tcount;  // instrumented runs: tiles per step
+    uint32_t epoch;            // entries carrying another epoch belong to a previous user of the slot
+    uint32_t pad_;
 };
+
+// Queue entry: epoch (8 bits) | job (24 bits) | local brick (32 bits).
+__host__ __device__ __forceinline__ unsigned long long make_entry(uint32_t epoch, uint32_t job, uint32_t lb) {
+    return ((unsigned long long)(epoch & 0xffu) << 56) | ((unsigned long long)(job & 0xffffffu) << 32) | lb;
+}
 
 // Mutable per-job state.
 struct JobState {
@@ -94,7 +103,7 @@ struct Ctl {
 struct SolveParams {
     Job* jobs;
     JobState* states;
-    unsigned long long* queue[3];  // entries (job << 32) | local brick
+    unsigned long long* queue[3];  // entries, see make_entry
     int32_t* stamps;               // per global brick: last iteration it was queued for
     Ctl* ctl;
     int32_t* map[2];               // optional dense per-voxel distance maps (per pair: job 0 / 1)

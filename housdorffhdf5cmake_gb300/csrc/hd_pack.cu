@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__
                 s.active = 0;
                 Job& J = jobs[P.job0 + j];
                 J.nbx = J.nby = J.nbz = 0;
+                J.epoch = P.epoch;
             }
         }
         return;
@@ -207,6 +208,7 @@ __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__
             J.brick0 = P.brick0[j];
             J.tstamp = P.tstamp[j];
             J.tcount = P.tcount[j];
+            J.epoch = P.epoch;
             JobState& s = states[P.job0 + j];
             s.sum = 0; s.remaining = rem[j]; s.bricks = 0; s.hd = 0; s.last_k = 0; s.status = 0;
             s.active = rem[j] > 0 ? 1 : 0;
@@ -244,7 +246,7 @@ __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__
             base = __shfl_sync(0xffffffffu, base, 0);
             if (have)
                 queue0[base + __popc(mball & ((1u << lane) - 1u))] =
-                    ((unsigned long long)(P.job0 + j) << 32) | (unsigned long long)t;
+                    make_entry(P.epoch, (uint32_t)(P.job0 + j), (uint32_t)t);
         }
     }
     (void)stats;

@@ -14,6 +14,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -115,6 +117,7 @@ struct hd_server {
     std::vector<Request*> slots;      // resident pair per slot
     std::vector<int> free_slots;
     std::vector<int> quarantine;      // slots freed during the last tick
+    std::vector<uint32_t> slot_epoch; // bumped on every admission into a slot
     RangeAlloc bricks;
     unsigned long long brick_cap = 0;
     // persistent device state
@@ -130,6 +133,7 @@ struct hd_server {
     int g_next = 1;
     hd_server_stats stats{};
     std::string err;
+    bool debug = false;  // HD_SERVER_DEBUG=1: one line per tick on stderr
 };
 
 namespace {
@@ -266,6 +270,7 @@ void tick(hd_server* s) {
         d.aligned = ((((uintptr_t)d.a) | ((uintptr_t)d.b)) & 15) == 0;
         d.kmax = r->kmax;
         d.job0 = 2 * r->slot;
+        d.epoch = ++s->slot_epoch[r->slot];
         d.info = (PairInfo*)(rb + r->off_info);
         descs.push_back(d);
         admitted.push_back(r);
@@ -336,15 +341,36 @@ void tick(hd_server* s) {
         if (resident > 0) s->g_next = std::max(s->g_next, hctl->g_end);
         hard_err = hctl->err;
     }
+    if (s->debug) {
+        std::fprintf(stderr,
+                     "[hd_server] tick %llu admitted %zu resident %d g_next %d err %d(%s) jobs_active %d q %u/%u/%u "
+                     "iters %d\n",
+                     (unsigned long long)s->stats.ticks, admitted.size(), resident, s->g_next, hctl->err,
+                     e == cudaSuccess ? "ok" : cudaGetErrorString(e), hctl->jobs_active, hctl->qcount[0],
+                     hctl->qcount[1], hctl->qcount[2], hctl->iters_run);
+        for (size_t sl = 0; sl < s->slots.size() && sl < 4; ++sl)
+            if (s->slots[sl])
+                std::fprintf(stderr, "[hd_server]   slot %zu: active %d/%d remaining %llu/%llu hd %d/%d status %d/%d\n", sl,
+                             hst[2 * sl].active, hst[2 * sl + 1].active, hst[2 * sl].remaining,
+                             hst[2 * sl + 1].remaining, hst[2 * sl].hd, hst[2 * sl + 1].hd, hst[2 * sl].status,
+                             hst[2 * sl + 1].status);
+    }
+    // A tick that admitted nothing and ran no step while jobs are still
+    // active means their frontier is empty with targets left, which the
+    // dilation cannot produce; fail those pairs rather than spin.
+    const bool stalled = hard_err == 0 && e == cudaSuccess && resident > 0 && admitted.empty() &&
+                         hctl->iters_run == 0 && hctl->jobs_active > 0;
+    if (stalled && s->debug) std::fprintf(stderr, "[hd_server] no progress: failing active pairs\n");
     std::vector<Request*> finished;
     for (size_t sl = 0; sl < s->slots.size(); ++sl) {
         Request* r = s->slots[sl];
         if (!r) continue;
         const JobState& s0 = hst[2 * sl];
         const JobState& s1 = hst[2 * sl + 1];
-        const bool fin = hard_err != 0 || r->cancel || (s0.active == 0 && s1.active == 0);
+        const bool fin = hard_err != 0 || stalled || r->cancel || (s0.active == 0 && s1.active == 0);
         if (fin) finished.push_back(r);
     }
+    if (stalled) hard_err = HD_ERR_ITER_LIMIT;
     unsigned long long cancelled_active = 0;
     for (Request* r : finished) {
         const size_t sl = (size_t)r->slot;
@@ -462,6 +488,7 @@ hd_status hd_server_create(hd_context* ctx, const hd_server_options* opt, hd_ser
         return HD_ERR_BAD_ARG;
     }
     s->se = s->opt.metric == HD_SE6 ? 0 : 1;
+    s->debug = std::getenv("HD_SERVER_DEBUG") != nullptr;
     int slots = s->opt.max_inflight > 0 ? s->opt.max_inflight : 1024;
     slots = std::min(slots, 16384);
     {
@@ -505,6 +532,7 @@ hd_status hd_server_create(hd_context* ctx, const hd_server_options* opt, hd_ser
         }
     }
     s->slots.assign(slots, nullptr);
+    s->slot_epoch.assign(slots, 0u);
     for (int i = slots - 1; i >= 0; --i) s->free_slots.push_back(i);
     s->worker = std::thread(worker_main, s);
     *out = s;

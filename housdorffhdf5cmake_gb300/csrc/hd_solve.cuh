@@ -104,13 +104,14 @@ __device__ __forceinline__ bool grid_step_barrier(Ctl* ctl, unsigned& gen, int g
 }
 
 template <int BXW, int BZ, bool SE18>
-__device__ __forceinline__ void brick_step(const SolveParams& p, int jid, unsigned lb, int g) {
+__device__ __forceinline__ void brick_step(const SolveParams& p, int jid, unsigned lb, unsigned epoch, int g) {
     constexpr int BY = 32 / BXW;
     const int lane = threadIdx.x & 31;
     const int lx = lane % BXW, ly = lane / BXW;
     JobState* st = p.states + jid;
     if (ld_relaxed_s32(&st->active) == 0) return;  // job finished: nothing left to cover
     const Job* Jp = p.jobs + jid;
+    if ((Jp->epoch & 0xffu) != epoch) return;      // left over from the slot's previous pair
     const int k = g - Jp->k0 + 1;  // local step, >= 1
     if (k > Jp->kmax) {
         if (lane == 0) {
@@ -222,10 +223,11 @@ __device__ __forceinline__ void brick_step(const SolveParams& p, int jid, unsign
             const int off = (z0 + i) * plane + rowoff;
             if (valid) {
                 dst[off] = nw;
-                const uint32_t u = uu[i];
-                const uint32_t hit = nw & u;
+                uint32_t hit = nw & uu[i];
                 if (hit) {
-                    U[off] = u & ~hit;
+                    // claim the hits: a voxel is counted once even if two warps
+                    // ever process the same brick in one step
+                    hit &= atomicAnd(&U[off], ~hit);
                     cnt += __popc(hit);
                     if (map != nullptr) {
                         const long long vz = Jp->oz + z0 + i, vyy = Jp->oy + y;
@@ -316,8 +318,7 @@ __device__ __forceinline__ void brick_step(const SolveParams& p, int jid, unsign
         if (lane == 0) base = atomicAdd(&p.ctl->qcount[qn], (unsigned)__popc(m));
         base = __shfl_sync(kFull, base, 0);
         if (need)
-            qdst[base + __popc(m & ((1u << lane) - 1u))] =
-                ((unsigned long long)jid << 32) | nlb;
+            qdst[base + __popc(m & ((1u << lane) - 1u))] = make_entry(epoch, (uint32_t)jid, nlb);
     }
 }
 
@@ -344,7 +345,7 @@ __global__ void __launch_bounds__(256, 2) solve_kernel(SolveParams p) {
             const unsigned long long* Q = qi == 0 ? p.queue[0] : (qi == 1 ? p.queue[1] : p.queue[2]);
             for (unsigned i = gw; i < cnt; i += nw) {
                 const unsigned long long e = Q[i];
-                brick_step<BXW, BZ, SE18>(p, (int)(e >> 32), (unsigned)e, g);
+                brick_step<BXW, BZ, SE18>(p, (int)((e >> 32) & 0xffffffu), (unsigned)e, (unsigned)(e >> 56), g);
             }
             const bool cont = grid_step_barrier(ctl, gen, g, p.timeout_ns, &s_flag);
             ++g;

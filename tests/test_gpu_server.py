@@ -69,7 +69,8 @@ def test_budget_admission_and_oversize(hd, ctx):
     pairs = _pairs(16, 13, lo=64, hi=96, edge=0.0)
     budget = 24 << 20  # a few pairs at a time
     with hd.Server(ctx, hbm_budget_bytes=budget) as srv:
-        big = torch.zeros((256, 256, 256), dtype=torch.uint8, device="cuda")
+        # 320^3: six 4.9 MB job buffers alone exceed the 24 MB budget
+        big = torch.zeros((320, 320, 320), dtype=torch.uint8, device="cuda")
         tbig = srv.submit(big, big)
         ts = [srv.submit(a, b) for a, b in pairs]
         res = [srv.wait(t, 60000) for t in ts]
