@@ -32,7 +32,7 @@ EXPORTS = (
     "hd_context_last_error", "hd_context_last_timings", "hd_compute_u8", "hd_compute_u8_device", "hd_batch_compute",
     "hd_profile_u8_device", "hd_distance_map_device", "hd_autotune", "hd_server_options_init",
     "hd_server_create", "hd_server_submit", "hd_server_poll", "hd_server_wait", "hd_server_cancel",
-    "hd_server_get_stats", "hd_server_destroy", "hd_load_hdf5_bool", "hd_free",
+    "hd_server_get_stats", "hd_server_destroy", "hd_compute_u8_device_noalloc", "hd_load_hdf5_bool", "hd_free",
 )
 
 
@@ -172,6 +172,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             "hd_server_cancel": (st, [vp, u64]),
             "hd_server_get_stats": (st, [vp, ctypes.POINTER(HdServerStats)]),
             "hd_server_destroy": (st, [vp]),
+            "hd_compute_u8_device_noalloc": (st, [vp, vp, i32, i32, i32, st, vp, vp]),
             "hd_load_hdf5_bool": (st, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(vp),
                                        ctypes.POINTER(ctypes.c_size_t)]),
             "hd_free": (None, [vp]),

@@ -209,6 +209,25 @@ typedef struct hd_server_stats {
 hd_status hd_server_get_stats(hd_server* srv, hd_server_stats* out);
 hd_status hd_server_destroy(hd_server* srv);
 
+/* ---- allocation-free variant ---------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they need a distance (all HBM handed to another allocator, a
+ * loop that must not call cudaMalloc/cudaFree, which can block and
+ * synchronise the device): hd_compute_u8_device with every intermediate buffer
+ * inside one fixed 80 MiB device array of the library (each GPU that loads the
+ * library holds it until exit).  No context, no allocation.  Masks and the
+ * result are the caller's DEVICE memory; the call only enqueues work on
+ * `stream` (cudaStream_t, NULL = legacy default stream) and *d_out is valid
+ * once the stream reaches it.  d_out->hd_robust uses the 0.95 percentile.
+ * Pairs whose buffers do not fit the array (about one byte per voxel;
+ * 512 x 512 x 256 fits) return HD_ERR_BAD_ARG before any work is enqueued.
+ * The first call on a device looks up the array's address with that device
+ * current: make it before any stream capture.  All calls share the array and
+ * it keeps the last call's contents (each call clears what must start at
+ * zero); calls that overlap on the GPU race on it. */
+hd_status hd_compute_u8_device_noalloc(const uint8_t* d_a, const uint8_t* d_b, int32_t W, int32_t H,
+                                       int32_t D, hd_metric metric, void* stream, hd_result* d_out);
+
 /* ---- HDF5 input (forBench/hdf5Manag.cu:44-86, loadHDFIntoBoolArr) -------- */
 /* Reads a rank-1 boolean dataset into a malloc'd byte array.  Returns
  * HD_ERR_UNSUPPORTED when the library was built without HDF5. */
