@@ -101,8 +101,10 @@ def _current_stream_ptr():
 class Context:
     """A device context of the library (hd_context_create).
 
-    Options mirror ``hd_options``: brick_x_words / brick_z (brick shape; 0 =
-    tuned), ctas_per_sm (0 = occupancy maximum), max_iterations (0 = W+H+D),
+    Options mirror ``hd_options``: kernel (1 = one dilation step per grid
+    barrier, 2 = temporally blocked; 0 = tuned/default), steps_per_barrier
+    (kernel 2: 1 or 2), brick_x_words / brick_z (brick shape; 0 = tuned),
+    ctas_per_sm (0 = occupancy maximum), max_iterations (0 = W+H+D),
     barrier_timeout_ns (0 = 10 s), percentile (robust HD, default 0.95),
     zero_copy (host masks read in place when the device can), tuning_table
     (JSON path of the autotuner's table).
@@ -110,7 +112,7 @@ class Context:
 
     def __init__(self, device: int = 0, *, brick_x_words=0, brick_z=0, ctas_per_sm=0, max_iterations=0,
                  barrier_timeout_ns=0, percentile=0.95, zero_copy=True, tuning_table=None,
-                 record_timings=False):
+                 record_timings=False, kernel=0, steps_per_barrier=0):
         L = N.load()
         opt = N.HdOptions()
         L.hd_options_init(ctypes.byref(opt))
@@ -124,6 +126,8 @@ class Context:
         self._tuning = tuning_table.encode() if tuning_table else None
         opt.tuning_table = self._tuning
         opt.record_timings = 1 if record_timings else 0
+        opt.kernel = int(kernel)
+        opt.steps_per_barrier = int(steps_per_barrier)
         h = ctypes.c_void_p()
         code = L.hd_context_create(int(device), ctypes.byref(opt), ctypes.byref(h))
         if code != HD_OK:

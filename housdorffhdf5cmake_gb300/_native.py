@@ -68,6 +68,8 @@ class HdOptions(ctypes.Structure):
         ("zero_copy", ctypes.c_int32),
         ("tuning_table", ctypes.c_char_p),
         ("record_timings", ctypes.c_int32),
+        ("kernel", ctypes.c_int32),
+        ("steps_per_barrier", ctypes.c_int32),
     ]
 
 
@@ -81,6 +83,9 @@ class HdTimings(ctypes.Structure):
         ("grid_ctas", ctypes.c_int32),
         ("brick_x_words", ctypes.c_int32),
         ("brick_z", ctypes.c_int32),
+        ("kernel", ctypes.c_int32),
+        ("steps_per_barrier", ctypes.c_int32),
+        ("brick_rows", ctypes.c_int32),
     ]
 
     def as_dict(self) -> dict:

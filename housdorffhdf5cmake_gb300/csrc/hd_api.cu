@@ -148,13 +148,18 @@ int robust_k(const uint64_t* hist, int len, uint64_t total, float p) {
     return len - 1;
 }
 
-int occupancy_of(hd_context* ctx, const void* fn) {
+int occupancy_of(hd_context* ctx, const void* fn, int threads, int smem) {
     auto it = ctx->occupancy.find(fn);
     if (it != ctx->occupancy.end()) return it->second;
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, 256, 0) != cudaSuccess) {
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) {
         cudaGetLastError();
-        n = 1;
+        return 0;
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
     }
     n = std::max(1, n);
     ctx->occupancy[fn] = n;
@@ -212,22 +217,27 @@ hd_status decode_result(const hdk::PairInfo& I, const hdk::JobState& s0, const h
     return (hd_status)st;
 }
 
-void pick_shape(hd_context* ctx, int se, const PairIn* pairs, int n, int* bxw, int* bz, int* cps) {
-    *bxw = 4;
-    *bz = 8;
-    *cps = 0;
+Shape pick_shape(hd_context* ctx, int se, const PairIn* pairs, int n) {
+    Shape sh;  // default: blocked kernel, 2 steps per barrier, 4 x 28 x 8 bricks
     double vox = 0;
     for (int i = 0; i < n; ++i) vox += (double)pairs[i].W * pairs[i].H * pairs[i].D;
     vox /= std::max(1, n);
     auto it = ctx->tune.entries.find(tune_key(se, vox, n));
-    if (it != ctx->tune.entries.end()) {
-        *bxw = it->second.bxw;
-        *bz = it->second.bz;
-        *cps = it->second.ctas_per_sm;
-    }
-    if (ctx->opt.brick_x_words > 0) *bxw = ctx->opt.brick_x_words;
-    if (ctx->opt.brick_z > 0) *bz = ctx->opt.brick_z;
-    if (ctx->opt.ctas_per_sm > 0) *cps = ctx->opt.ctas_per_sm;
+    if (it != ctx->tune.entries.end()) sh = it->second.shape;
+    const hd_options& o = ctx->opt;
+    if (o.kernel == 1 || o.kernel == 2) sh.kernel = o.kernel;
+    if (o.kernel == 0 && o.brick_x_words > 0 && o.steps_per_barrier == 0) sh.kernel = 1;
+    if (o.brick_x_words > 0) sh.bxw = o.brick_x_words;
+    if (o.brick_z > 0) sh.bz = o.brick_z;
+    if (o.steps_per_barrier > 0) sh.steps = o.steps_per_barrier;
+    if (o.ctas_per_sm > 0) sh.ctas_per_sm = o.ctas_per_sm;
+    sh.finish();
+    return sh;
+}
+
+const void* solve_fn_of(int se, const Shape& sh) {
+    if (sh.kernel == 2) return hdk::solve_tb_kernel_ptr(se, sh.steps, sh.bz);
+    return hdk::solve_kernel_ptr(se, sh.bxw, sh.bz);
 }
 
 hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s, const RunOpts& ro,
@@ -235,19 +245,22 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     if (n <= 0) return HD_OK;
     if (n > hdk::kMaxPairsPerLaunch) return set_error(ctx, HD_ERR_BAD_ARG, "too many pairs in one launch");
     const int se = ro.se;
-    int bxw = ro.bxw, bz = ro.bz, cps = ro.ctas_per_sm;
-    {
-        int tb, tz, tc;
-        pick_shape(ctx, se, pairs, n, &tb, &tz, &tc);
-        if (!bxw) bxw = tb;
-        if (!bz) bz = tz;
-        if (!cps) cps = tc;
-    }
-    const void* solve_fn = hdk::solve_kernel_ptr(se, bxw, bz);
-    if (!solve_fn)
-        return set_error(ctx, HD_ERR_BAD_ARG, "brick shape %d words x %d planes not compiled in", bxw, bz);
-    const int by = 32 / bxw;
     const bool stats = ro.stats != 0;
+    Shape sh = ro.force_shape ? ro.shape : pick_shape(ctx, se, pairs, n);
+    if (stats || ro.map_a || ro.map_b) {
+        // instrumented runs and per-voxel maps are implemented by the one-step kernel
+        if (sh.kernel != 1) {
+            sh.kernel = 1;
+            sh.bxw = 4;
+            sh.bz = 8;
+        }
+    }
+    sh.finish();
+    const void* solve_fn = solve_fn_of(se, sh);
+    if (!solve_fn)
+        return set_error(ctx, HD_ERR_BAD_ARG, "kernel %d with %d words x %d rows x %d planes (%d steps) not compiled in",
+                         sh.kernel, sh.bxw, sh.by, sh.bz, sh.steps);
+    const int bxw = sh.bxw, by = sh.by, bz = sh.bz, cps = sh.ctas_per_sm;
 
     // ---- layout --------------------------------------------------------
     std::vector<PairPlan> plan(n);
@@ -403,7 +416,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
                                  (unsigned long long*)(dbase + off_q[1]),
                                  (unsigned long long*)(dbase + off_q[2])};
     if (timing) cudaEventRecord(ctx->ev[1], s);
-    e = hdk::launch_setup(ddesc, n, grid_x, djobs, dstates, dq[g0 % 3], dctl, g0, bxw, bz, stats ? 1 : 0, s);
+    e = hdk::launch_setup(ddesc, n, grid_x, djobs, dstates, dq[g0 % 3], dctl, g0, bxw, by, bz, stats ? 1 : 0, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "setup launch");
     if (ro.map_a || ro.map_b) {
         e = hdk::launch_map_init(ddesc, ro.map_a, ro.map_b,
@@ -424,15 +437,16 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     sp.map_h = pairs[0].H;
     sp.map_d = pairs[0].D;
     sp.g0 = g0;
-    sp.max_iters = kmax_all + 2;
+    sp.max_iters = kmax_all / sh.steps + 2;
     sp.stats = stats ? 1 : 0;
     sp.timeout_ns = ctx->opt.barrier_timeout_ns > 0 ? ctx->opt.barrier_timeout_ns : 10000000000LL;
-    const int occ = occupancy_of(ctx, solve_fn);
+    const int occ = occupancy_of(ctx, solve_fn, sh.threads, sh.smem);
+    if (occ <= 0) return set_error(ctx, HD_ERR_CUDA, "dilation kernel cannot be made resident");
     const int per_sm = cps > 0 ? std::min(cps, occ) : occ;
-    dim3 grid(ctx->sm_count * per_sm), block(256);
+    dim3 grid(ctx->sm_count * per_sm), block(sh.threads);
     void* args[] = {&sp};
     if (timing) cudaEventRecord(ctx->ev[2], s);
-    e = cudaLaunchCooperativeKernel(solve_fn, grid, block, args, 0, s);
+    e = cudaLaunchCooperativeKernel(solve_fn, grid, block, args, (size_t)sh.smem, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "dilation launch");
     if (timing) cudaEventRecord(ctx->ev[3], s);
 
@@ -471,6 +485,9 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         T.grid_ctas = (int)grid.x;
         T.brick_x_words = bxw;
         T.brick_z = bz;
+        T.kernel = sh.kernel;
+        T.steps_per_barrier = sh.steps;
+        T.brick_rows = by;
     }
     const float pct = (ctx->opt.percentile > 0.f && ctx->opt.percentile <= 1.f) ? ctx->opt.percentile : 0.95f;
     hd_status first = HD_OK;
@@ -513,6 +530,9 @@ using namespace hdh;
 namespace hdk {
 const void* solve_kernel_ptr(int se, int bxw, int bz) {
     return se == 0 ? solve_kernel_ptr_se6(bxw, bz) : solve_kernel_ptr_se18(bxw, bz);
+}
+const void* solve_tb_kernel_ptr(int se, int steps, int bz) {
+    return se == 0 ? solve_tb_kernel_ptr_se6(steps, bz) : solve_tb_kernel_ptr_se18(steps, bz);
 }
 }  // namespace hdk
 

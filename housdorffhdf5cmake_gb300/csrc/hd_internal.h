@@ -28,11 +28,38 @@ struct PinnedArena {
     void release();
 };
 
-// One tuned brick shape per (element, volume class).
-struct TuneEntry {
+// Dilation kernel and brick geometry.
+//   kernel 1: one step per grid barrier, bricks bxw words x 32/bxw rows x bz planes
+//   kernel 2: `steps` steps per grid barrier, bricks 4 words x (32 - 2 steps) rows x bz planes
+struct Shape {  // default: the autotuner's choice on the 512x512x256, 512^3 and ragged-batch workloads
+    int kernel = 2;
     int bxw = 4;
+    int by = 28;
     int bz = 8;
+    int steps = 2;
     int ctas_per_sm = 0;
+    int threads = 128;  // CTA size of the persistent launch
+    int smem = 0;       // dynamic shared memory per CTA
+    void finish() {
+        if (kernel == 2) {
+            // 4 warps per CTA, each staging (bz + 2 steps) planes x 32 rows x 32 B
+            // of state and bz x 32 rows x 16 B of uncovered-target words
+            bxw = 4;
+            by = 32 - 2 * steps;
+            threads = 128;
+            smem = 4 * ((bz + 2 * steps) * 32 * 32 + bz * 32 * 16);
+        } else {
+            by = 32 / bxw;
+            steps = 1;
+            threads = 256;
+            smem = 0;
+        }
+    }
+};
+
+// One tuned shape per (element, volume class).
+struct TuneEntry {
+    Shape shape;
     double us = 0.0;  // measured time of the winner (informational)
 };
 
@@ -96,7 +123,8 @@ struct RunOpts {
     uint64_t* tiles_ba = nullptr;
     int32_t tiles_len = 0;
     uint64_t* bricks = nullptr;
-    int bxw = 0, bz = 0, ctas_per_sm = 0;  // 0 = from options / tuning table
+    bool force_shape = false;  // use `shape` as given (autotuner)
+    Shape shape;
 };
 
 hd_status set_error(hd_context* ctx, hd_status st, const char* fmt, ...);
@@ -115,8 +143,11 @@ const uint8_t* zero_copy_ptr(hd_context* ctx, const uint8_t* p);
 hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s, const RunOpts& ro,
                     hd_result* out);
 
-// Brick shape for a workload (options, then tuning table, then default).
-void pick_shape(hd_context* ctx, int se, const PairIn* pairs, int n, int* bxw, int* bz, int* cps);
+// Kernel and brick shape for a workload (options, then tuning table, then default).
+Shape pick_shape(hd_context* ctx, int se, const PairIn* pairs, int n);
+
+// Host stub of the persistent kernel of a shape (nullptr if not compiled in).
+const void* solve_fn_of(int se, const Shape& sh);
 
 // Pair result from the packing counts and the two jobs' states (s0 dilates A
 // and covers B, s1 the reverse) and their per-step histograms.
@@ -124,8 +155,10 @@ hd_status decode_result(const hdk::PairInfo& I, const hdk::JobState& s0, const h
                         const uint64_t* hist_ab, const uint64_t* hist_ba, int kp1, int iters, int err,
                         float pct, hd_result* out);
 
-// Resident CTAs per SM of a persistent kernel (cached per context).
-int occupancy_of(hd_context* ctx, const void* fn);
+// Resident CTAs per SM of a persistent kernel launched with `threads` threads
+// and `smem` bytes of dynamic shared memory (cached per context; raises the
+// kernel's dynamic shared memory limit first when needed).
+int occupancy_of(hd_context* ctx, const void* fn, int threads, int smem);
 
 // Percentile HD of one direction with the reference's float stopping rule.
 int robust_k(const uint64_t* hist, int len, uint64_t total, float p);

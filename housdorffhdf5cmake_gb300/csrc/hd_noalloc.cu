@@ -221,7 +221,8 @@ extern "C" hd_status hd_compute_u8_device_noalloc(const uint8_t* d_a, const uint
     hdk::Ctl* ctl = (hdk::Ctl*)(base + L.ctl);
     unsigned long long* q[3] = {(unsigned long long*)(base + L.queue[0]), (unsigned long long*)(base + L.queue[1]),
                                 (unsigned long long*)(base + L.queue[2])};
-    if (e == cudaSuccess) e = hdk::launch_setup(desc, 1, grid_x, jobs, states, q[g0 % 3], ctl, g0, kBxw, kBz, 0, s);
+    if (e == cudaSuccess)
+        e = hdk::launch_setup(desc, 1, grid_x, jobs, states, q[g0 % 3], ctl, g0, kBxw, 32 / kBxw, kBz, 0, s);
     if (e == cudaSuccess) {
         hdk::SolveParams sp{};
         sp.jobs = jobs;

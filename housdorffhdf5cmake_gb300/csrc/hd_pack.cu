@@ -161,10 +161,9 @@ __device__ __forceinline__ Domain make_domain(const PairDesc& P, const PairInfo&
 // grid (X, npairs), block 256.
 __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__ descs, Job* jobs,
                                                     JobState* states, unsigned long long* queue0,
-                                                    Ctl* ctl, int g0, int bxw, int bz, int stats) {
+                                                    Ctl* ctl, int g0, int bxw, int by, int bz, int stats) {
     const PairDesc& P = descs[blockIdx.y];
     const PairInfo I = *P.info;
-    const int by = 32 / bxw;
     const bool empty_a = I.n_a == 0, empty_b = I.n_b == 0;
     const unsigned long long rem[2] = {I.n_b - I.n_ab, I.n_a - I.n_ab};
     const long long tid0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -284,10 +283,10 @@ cudaError_t launch_pack(const PairDesc* d_descs, int npairs, int grid_x, cudaStr
 }
 
 cudaError_t launch_setup(const PairDesc* d_descs, int npairs, int grid_x, Job* jobs, JobState* states,
-                         unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int bz, int stats,
+                         unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz, int stats,
                          cudaStream_t s) {
     dim3 grid(grid_x, npairs);
-    setup_kernel<<<grid, 256, 0, s>>>(d_descs, jobs, states, queue0, ctl, g0, bxw, bz, stats);
+    setup_kernel<<<grid, 256, 0, s>>>(d_descs, jobs, states, queue0, ctl, g0, bxw, by, bz, stats);
     return cudaGetLastError();
 }
 

@@ -103,7 +103,8 @@ inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 struct hd_server {
     hd_context* ctx = nullptr;
     hd_server_options opt{};
-    int se = 0, bxw = 4, bz = 8, grid = 0;
+    int se = 0, grid = 0;
+    Shape shape;
     const void* solve_fn = nullptr;
     cudaStream_t stream = nullptr;
     std::thread worker;
@@ -147,12 +148,12 @@ hd_status cuda_err(hd_server* s, cudaError_t e, const char* where) {
 // Sizes of one request's device memory (resident part lives until completion,
 // transient part only through packing and set-up).
 void plan_request(hd_server* s, Request* r) {
-    const int by = 32 / s->bxw;
+    const int by = s->shape.by;
     r->wxf = (r->W + 31) / 32;
     const long long pitch = (r->wxf + 3) / 4 * 4;
     r->dom_words = pitch * r->H * r->D;
-    r->nbricks = (unsigned long long)((r->wxf + s->bxw - 1) / s->bxw) * ((r->H + by - 1) / by) *
-                 ((r->D + s->bz - 1) / s->bz);
+    r->nbricks = (unsigned long long)((r->wxf + s->shape.bxw - 1) / s->shape.bxw) * ((r->H + by - 1) / by) *
+                 ((r->D + s->shape.bz - 1) / s->shape.bz);
     r->kmax = r->W + r->H + r->D;
     const size_t job_bytes = align_up(4ULL * r->dom_words);
     r->off_hist = 6 * job_bytes;
@@ -294,7 +295,8 @@ void tick(hd_server* s) {
         if (e == cudaSuccess) e = hdk::launch_pack(s->d_descs, (int)admitted.size(), gx, st);
         if (e == cudaSuccess)
             e = hdk::launch_setup(s->d_descs, (int)admitted.size(), gx, s->d_jobs, s->d_states,
-                                  s->d_queue[s->g_next % 3], s->d_ctl, s->g_next, s->bxw, s->bz, 0, st);
+                                  s->d_queue[s->g_next % 3], s->d_ctl, s->g_next, s->shape.bxw, s->shape.by,
+                                  s->shape.bz, 0, st);
         // pageable sources of cudaMemcpyAsync and the info initialisers must
         // outlive the copies: wait for the admission work before going on
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -322,7 +324,8 @@ void tick(hd_server* s) {
         sp.max_iters = s->opt.tick_iterations;
         sp.timeout_ns = s->ctx->opt.barrier_timeout_ns > 0 ? s->ctx->opt.barrier_timeout_ns : 10000000000LL;
         void* args[] = {&sp};
-        e = cudaLaunchCooperativeKernel(s->solve_fn, dim3(s->grid), dim3(256), args, 0, st);
+        e = cudaLaunchCooperativeKernel(s->solve_fn, dim3(s->grid), dim3(s->shape.threads), args,
+                                        (size_t)s->shape.smem, st);
     }
     // ---- read back states, complete finished pairs ---------------------------
     const size_t nst = 2 * s->slots.size();
@@ -499,17 +502,22 @@ hd_status hd_server_create(hd_context* ctx, const hd_server_options* opt, hd_ser
             return HD_ERR_CUDA;
         }
         PairIn typical{nullptr, nullptr, 256, 256, 160, nullptr, nullptr};
-        int cps = 0;
-        pick_shape(ctx, s->se, &typical, 16, &s->bxw, &s->bz, &cps);
-        s->solve_fn = hdk::solve_kernel_ptr(s->se, s->bxw, s->bz);
+        s->shape = pick_shape(ctx, s->se, &typical, 16);
+        const int cps = s->shape.ctas_per_sm;
+        s->solve_fn = solve_fn_of(s->se, s->shape);
         if (!s->solve_fn) {
             delete s;
             return HD_ERR_BAD_ARG;
         }
-        const int occ = occupancy_of(ctx, s->solve_fn);
+        const int occ = occupancy_of(ctx, s->solve_fn, s->shape.threads, s->shape.smem);
+        if (occ <= 0) {
+            delete s;
+            return HD_ERR_CUDA;
+        }
         s->grid = ctx->sm_count * (cps > 0 ? std::min(cps, occ) : occ);
-        // brick ids: one per 3 KB of budget (a job brick holds 3 x 1 KB words), capped
-        s->brick_cap = std::min<unsigned long long>(s->opt.hbm_budget_bytes / 3072ULL, 1ULL << 26);
+        // brick ids: one per 3 x (brick bytes) of budget (each job brick spans 3 buffers), capped
+        const unsigned long long brick_bytes = 4ULL * s->shape.bxw * s->shape.by * s->shape.bz;
+        s->brick_cap = std::min<unsigned long long>(s->opt.hbm_budget_bytes / (3 * brick_bytes) + 4096, 1ULL << 26);
         s->bricks = RangeAlloc(s->brick_cap);
         cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaMalloc(&s->d_jobs, sizeof(Job) * 2 * slots);

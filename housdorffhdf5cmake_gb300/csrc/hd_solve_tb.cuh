@@ -1,0 +1,357 @@
+// hd_solve_tb.cuh -- temporally blocked frontier dilation: T steps per grid
+// barrier (sm_103a).
+//
+// Same job model, queues, stamps, ping-pong buffers and barrier as
+// hd_solve.cuh, but one queue item advances a brick by T dilation steps:
+//
+//   brick     IW = 4 words (128 voxels) in x  x  32 - 2T rows  x  BZ planes
+//   warp      lane = one row: the 4 interior words plus one halo word on
+//             each side, rows y0 - T .. y0 + 32 - T - 1 (T halo rows above
+//             and below the interior), streamed plane by plane along z from
+//             z0 - T to z0 + BZ + T - 1
+//   levels    level 0 is the loaded state; level s is the state after s
+//             steps, computed one plane behind level s - 1 from a window of
+//             three of its planes; rows come from the neighbouring lanes by
+//             shuffle, x carries from the neighbouring words of the row
+//
+// Level s is exact on rows [s, 32 - s) and planes [s, BZ + 2T - s) of the
+// streamed block (errors from the unknown outside creep in one voxel per
+// step; the halo word absorbs x for T < 32), so the interior is exact for all
+// s <= T.  At every level the interior is cover-tested (hits are counted with
+// step k_base + s, the distance of those voxels) and the final level is
+// written to the other ping-pong buffer.
+//
+// Frontier rule: a brick is queued for the next iteration iff its state or
+// the part of a neighbour within reach of its halo (the adjacent word in x,
+// T rows / planes in y / z) changed during this iteration.  A brick not
+// queued has D^{(i+1)T} = D^{iT} on itself and its halo, so its next T steps
+// change nothing and both ping-pong buffers already hold its state.
+#pragma once
+#include "hd_solve.cuh"
+
+namespace hdk {
+
+// Shared memory per warp: the streamed rows (32 B each: 4 interior words,
+// the two halo words, 2 pad words) for NP planes, and the interior
+// uncovered-target words (16 B per row) for BZ planes.
+template <int T, int BZ>
+struct TbSmem {
+    static constexpr int NP = BZ + 2 * T;
+    static constexpr int kRowBytes = 32;
+    static constexpr int kURowBytes = 16;
+    static constexpr int kInBytes = NP * 32 * kRowBytes;
+    static constexpr int kWarpBytes = kInBytes + BZ * 32 * kURowBytes;
+};
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void* src, uint32_t src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+template <int T, int BZ, bool SE18>
+__device__ __forceinline__ void brick_tb(const SolveParams& p, int jid, unsigned lb, unsigned epoch, int g,
+                                         unsigned char* wsm) {
+    constexpr int IW = 4;
+    constexpr int NW = IW + 2;
+    constexpr int BYI = 32 - 2 * T;
+    constexpr int NP = BZ + 2 * T;
+    using SM = TbSmem<T, BZ>;
+    const int lane = threadIdx.x & 31;
+    JobState* st = p.states + jid;
+    if (ld_relaxed_s32(&st->active) == 0) return;
+    const Job* Jp = p.jobs + jid;
+    if ((Jp->epoch & 0xffu) != epoch) return;
+    const int iter = g - Jp->k0;  // this job's iteration index, 0-based
+    const int kb = iter * T;      // steps completed before this iteration
+    if (kb + 1 > Jp->kmax) {
+        if (lane == 0) {
+            st->status = kErrIterLimit;
+            atomicCAS(&p.ctl->err, 0, kErrIterLimit);
+        }
+        return;
+    }
+    const int nbx = Jp->nbx, nby = Jp->nby, nbz = Jp->nbz;
+    const int Wx = Jp->wx, Hd = Jp->h, Dd = Jp->d;
+    const int bx = (int)(lb % (unsigned)nbx);
+    const unsigned tq = lb / (unsigned)nbx;
+    const int by = (int)(tq % (unsigned)nby);
+    const int bz = (int)(tq / (unsigned)nby);
+    const int wx0 = bx * IW, y0 = by * BYI, z0 = bz * BZ;
+    const int y = y0 - T + lane;
+    const bool rowv = y >= 0 && y < Hd;
+    const bool inter = rowv && lane >= T && lane < 32 - T;
+    const uint32_t* __restrict__ src = Jp->buf[iter & 1];
+    uint32_t* __restrict__ dst = Jp->buf[(iter + 1) & 1];
+    uint32_t* __restrict__ U = Jp->U;
+    const int pitch = Jp->pitch;
+    const int plane = pitch * Hd;
+    const int rowoff = (rowv ? y : 0) * pitch + wx0;
+    const bool hl_ok = rowv && wx0 > 0;
+    const bool hr_ok = rowv && wx0 + IW < Wx;
+    uint32_t wm[NW];  // valid bits of each word of this lane's row
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+        const int w = wx0 - 1 + j;
+        wm[j] = (rowv && w >= 0 && w < Wx) ? (w == Wx - 1 ? Jp->tailmask : kFull) : 0u;
+    }
+
+    // Stage this lane's rows: every copy of the brick is in flight at once;
+    // rows, planes and halo words outside the domain are zero-filled.
+    const uint32_t s_in = (uint32_t)__cvta_generic_to_shared(wsm);
+    const uint32_t s_u = s_in + SM::kInBytes;
+#pragma unroll
+    for (int r = 0; r < NP; ++r) {
+        const int z = z0 - T + r;
+        const bool ok = rowv && z >= 0 && z < Dd;
+        const uint32_t* gp = src + (ok ? z * plane + rowoff : 0);
+        const uint32_t d = s_in + (uint32_t)((r * 32 + lane) * SM::kRowBytes);
+        cp_async16(d, gp, ok ? 16u : 0u);
+        cp_async4(d + 16, (ok && hl_ok) ? gp - 1 : gp, (ok && hl_ok) ? 4u : 0u);
+        cp_async4(d + 20, (ok && hr_ok) ? gp + IW : gp, (ok && hr_ok) ? 4u : 0u);
+    }
+#pragma unroll
+    for (int i = 0; i < BZ; ++i) {
+        const int z = z0 + i;
+        const bool ok = inter && z < Dd;
+        cp_async16(s_u + (uint32_t)((i * 32 + lane) * SM::kURowBytes), U + (ok ? z * plane + rowoff : 0),
+                   ok ? 16u : 0u);
+    }
+    cp_async_wait_all();  // each lane reads back only its own rows
+
+    auto plane_ok = [&](int r) {  // streamed plane index r -> inside the domain
+        const int z = z0 - T + r;
+        return z >= 0 && z < Dd;
+    };
+    auto in_row = [&](int r) -> const uint32_t* {
+        return reinterpret_cast<const uint32_t*>(wsm + (r * 32 + lane) * SM::kRowBytes);
+    };
+    auto u_row = [&](int i) -> uint32_t* {
+        return reinterpret_cast<uint32_t*>(wsm + SM::kInBytes + (i * 32 + lane) * SM::kURowBytes);
+    };
+    auto load_row = [&](int r, uint32_t (&C)[NW]) {
+        const uint32_t* rp = in_row(r);
+        const uint4 v = *reinterpret_cast<const uint4*>(rp);
+        const uint2 h = *reinterpret_cast<const uint2*>(rp + 4);
+        C[0] = h.x & wm[0];
+        C[1] = v.x & wm[1];
+        C[2] = v.y & wm[2];
+        C[3] = v.z & wm[3];
+        C[4] = v.w & wm[4];
+        C[5] = h.y & wm[5];
+    };
+    // In-plane terms of one level's plane: M = C | sx(C) | sy(C) [| sx(sy(C))],
+    // Z = C [| sx(sy(C))]: what the plane contributes to itself and to the
+    // planes above and below.
+    auto terms = [&](const uint32_t (&C)[NW], uint32_t (&M)[NW], uint32_t (&Z)[NW]) {
+        uint32_t Y[NW];
+#pragma unroll
+        for (int j = 0; j < NW; ++j) {
+            uint32_t up = __shfl_up_sync(kFull, C[j], 1);
+            uint32_t dn = __shfl_down_sync(kFull, C[j], 1);
+            if (lane == 0) up = 0u;
+            if (lane == 31) dn = 0u;
+            Y[j] = up | dn;
+        }
+#pragma unroll
+        for (int j = 0; j < NW; ++j) {
+            const uint32_t l = j > 0 ? C[j - 1] : 0u, r = j < NW - 1 ? C[j + 1] : 0u;
+            const uint32_t sx = (C[j] << 1) | (l >> 31) | (C[j] >> 1) | (r << 31);
+            if constexpr (!SE18) {
+                M[j] = C[j] | sx | Y[j];
+                Z[j] = C[j];
+            } else {
+                const uint32_t yl = j > 0 ? Y[j - 1] : 0u, yr = j < NW - 1 ? Y[j + 1] : 0u;
+                const uint32_t sxy = (Y[j] << 1) | (yl >> 31) | (Y[j] >> 1) | (yr << 31);
+                M[j] = C[j] | sx | Y[j] | sxy;
+                Z[j] = C[j] | sxy;
+            }
+        }
+    };
+
+    // Register windows of levels 0 .. T-1: M of the last two planes, Z of the
+    // last three.
+    uint32_t Mw[T][2][NW], Zw[T][3][NW];
+    unsigned cnt[T];
+#pragma unroll
+    for (int s = 0; s < T; ++s) cnt[s] = 0;
+    uint32_t d_any = 0, d_xl = 0, d_xh = 0, d_zl = 0, d_zh = 0, u_hits = 0;
+    const bool band_yl = inter && (lane - T) < T;
+    const bool band_yh = inter && (lane - T) >= BYI - T;
+
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+        {
+            uint32_t C[NW];
+            load_row(q, C);
+            terms(C, Mw[0][q % 2], Zw[0][q % 3]);
+        }
+#pragma unroll
+        for (int s = 1; s <= T; ++s) {
+            const int r = q - s;
+            if (r >= s && r <= NP - 1 - s) {
+                uint32_t out[NW];
+                const bool pv = plane_ok(r);
+#pragma unroll
+                for (int j = 0; j < NW; ++j)
+                    out[j] = pv ? ((Mw[s - 1][r % 2][j] | Zw[s - 1][(r + 2) % 3][j] | Zw[s - 1][(r + 1) % 3][j]) &
+                                   wm[j])
+                                : 0u;
+                if (r >= T && r < T + BZ) {
+                    // cover test of the interior at step kb + s (U rows of
+                    // non-interior lanes and planes are zero)
+                    uint32_t* ur = u_row(r - T);
+                    uint4 u = *reinterpret_cast<const uint4*>(ur);
+                    const uint32_t h0 = out[1] & u.x, h1 = out[2] & u.y, h2 = out[3] & u.z, h3 = out[4] & u.w;
+                    const uint32_t hany = h0 | h1 | h2 | h3;
+                    if (hany) {
+                        cnt[s - 1] += __popc(h0) + __popc(h1) + __popc(h2) + __popc(h3);
+                        u.x &= ~h0;
+                        u.y &= ~h1;
+                        u.z &= ~h2;
+                        u.w &= ~h3;
+                        *reinterpret_cast<uint4*>(ur) = u;
+                        u_hits |= 1u << (r - T);
+                    }
+                }
+                if (s < T) {
+                    terms(out, Mw[s][r % 2], Zw[s][r % 3]);
+                } else {
+                    // final level: store, write back U, record changes
+                    const int z = z0 - T + r;
+                    if (inter && z < Dd) {
+                        const int off = z * plane + rowoff;
+                        *reinterpret_cast<uint4*>(dst + off) = make_uint4(out[1], out[2], out[3], out[4]);
+                        const uint4 c0 = *reinterpret_cast<const uint4*>(in_row(r));
+                        const uint32_t dx0 = out[1] ^ (c0.x & wm[1]), dx3 = out[4] ^ (c0.w & wm[4]);
+                        const uint32_t dall = dx0 | (out[2] ^ (c0.y & wm[2])) | (out[3] ^ (c0.z & wm[3])) | dx3;
+                        if (u_hits & (1u << (r - T)))
+                            *reinterpret_cast<uint4*>(U + off) = *reinterpret_cast<const uint4*>(u_row(r - T));
+                        d_any |= dall;
+                        d_xl |= dx0;
+                        d_xh |= dx3;
+                        if (r - T < T) d_zl |= dall;
+                        if (r - T >= BZ - T) d_zh |= dall;
+                    }
+                }
+            }
+        }
+    }
+
+    // per-step hit counts
+#pragma unroll
+    for (int s = 0; s < T; ++s) {
+        unsigned c = cnt[s];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+        cnt[s] = c;
+    }
+    if (lane == 0) {
+        unsigned long long tot = 0;
+#pragma unroll
+        for (int s = 0; s < T; ++s) {
+            if (cnt[s]) {
+                const int k = kb + s + 1;
+                tot += cnt[s];
+                atomicAdd(&st->sum, (unsigned long long)k * cnt[s]);
+                atomicMax(&st->hd, k);
+                atomicAdd(&Jp->hist[k], (unsigned long long)cnt[s]);
+            }
+        }
+        if (tot) {
+            const unsigned long long left = atomicAdd(&st->remaining, (unsigned long long)(-(long long)tot));
+            if (left == tot) {
+                st->active = 0;
+                atomicSub(&p.ctl->jobs_active, 1);
+            }
+        }
+        if (p.stats) atomicAdd(&st->bricks, 1ull);
+    }
+
+    // frontier
+    if (!__any_sync(kFull, d_any != 0)) return;
+    const bool fxl = __any_sync(kFull, d_xl != 0);
+    const bool fxh = __any_sync(kFull, d_xh != 0);
+    const bool fyl = __any_sync(kFull, band_yl && d_any != 0);
+    const bool fyh = __any_sync(kFull, band_yh && d_any != 0);
+    const bool fzl = __any_sync(kFull, d_zl != 0);
+    const bool fzh = __any_sync(kFull, d_zh != 0);
+    bool need = false;
+    unsigned nlb = 0;
+    if (lane < 27) {
+        const int ox = lane % 3 - 1, oy = (lane / 3) % 3 - 1, oz = lane / 9 - 1;
+        const int nnz = (ox != 0) + (oy != 0) + (oz != 0);
+        need = SE18 || T > 1 || nnz <= 1;
+        if (ox < 0) need = need && fxl;
+        if (ox > 0) need = need && fxh;
+        if (oy < 0) need = need && fyl;
+        if (oy > 0) need = need && fyh;
+        if (oz < 0) need = need && fzl;
+        if (oz > 0) need = need && fzh;
+        const int nx = bx + ox, ny = by + oy, nz = bz + oz;
+        need = need && nx >= 0 && nx < nbx && ny >= 0 && ny < nby && nz >= 0 && nz < nbz;
+        if (need) {
+            nlb = (unsigned)((nz * nby + ny) * nbx + nx);
+            need = atomicMax(&p.stamps[Jp->brick0 + nlb], g + 1) < g + 1;
+        }
+    }
+    const unsigned m = __ballot_sync(kFull, need);
+    if (m) {
+        const int qn = (g + 1) % 3;
+        unsigned long long* qdst = qn == 0 ? p.queue[0] : (qn == 1 ? p.queue[1] : p.queue[2]);
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(&p.ctl->qcount[qn], (unsigned)__popc(m));
+        base = __shfl_sync(kFull, base, 0);
+        if (need) qdst[base + __popc(m & ((1u << lane) - 1u))] = make_entry(epoch, (uint32_t)jid, nlb);
+    }
+}
+
+constexpr int kTbWarps = 4;  // warps per CTA of the blocked kernel
+
+template <int T, int BZ, bool SE18>
+__global__ void __launch_bounds__(kTbWarps * 32) solve_tb_kernel(SolveParams p) {
+    extern __shared__ __align__(16) unsigned char tb_smem[];
+    __shared__ int s_flag;
+    __shared__ unsigned s_gen, s_cnt;
+    Ctl* ctl = p.ctl;
+    if (threadIdx.x == 0) {
+        s_gen = ld_acquire_u32(&ctl->bar_gen);
+        s_cnt = ld_relaxed_u32(&ctl->qcount[p.g0 % 3]);
+    }
+    __syncthreads();
+    unsigned gen = s_gen;
+    unsigned cnt = s_cnt;
+    const int wpb = blockDim.x >> 5;
+    const unsigned gw = blockIdx.x * wpb + (threadIdx.x >> 5);
+    const unsigned nw = gridDim.x * wpb;
+    int g = p.g0;
+    int it = 0;
+    if (cnt > 0) {
+        for (;;) {
+            const int qi = g % 3;
+            const unsigned long long* Q = qi == 0 ? p.queue[0] : (qi == 1 ? p.queue[1] : p.queue[2]);
+            for (unsigned i = gw; i < cnt; i += nw) {
+                const unsigned long long e = Q[i];
+                brick_tb<T, BZ, SE18>(p, (int)((e >> 32) & 0xffffffu), (unsigned)e, (unsigned)(e >> 56), g,
+                                      tb_smem + (threadIdx.x >> 5) * TbSmem<T, BZ>::kWarpBytes);
+            }
+            const bool cont = grid_step_barrier(ctl, gen, g, p.timeout_ns, &s_flag);
+            ++g;
+            ++it;
+            if (!cont || it >= p.max_iters) break;
+            if (threadIdx.x == 0) s_cnt = ld_relaxed_u32(&ctl->qcount[g % 3]);
+            __syncthreads();
+            cnt = s_cnt;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctl->g_end = g;
+        ctl->iters_run = it;
+    }
+}
+
+}  // namespace hdk

@@ -1,0 +1,19 @@
+// hd_solve_tb_se18.cu -- instantiations of the temporally blocked dilation
+// kernel for the 18-neighbour structuring element.
+#include "hd_kernels.h"
+#include "hd_solve_tb.cuh"
+
+namespace hdk {
+
+#define HD_TB_CASE(T, BZ) \
+    if (steps == T && bz == BZ) return reinterpret_cast<const void*>(&solve_tb_kernel<T, BZ, true>);
+
+const void* solve_tb_kernel_ptr_se18(int steps, int bz) {
+    HD_TB_CASE(1, 8)
+    HD_TB_CASE(1, 16)
+    HD_TB_CASE(2, 8)
+    HD_TB_CASE(2, 16)
+    return nullptr;
+}
+
+}  // namespace hdk

@@ -39,9 +39,10 @@ bool TuneTable::save(const std::string& path) const {
     f << "{\n  \"version\": 1,\n  \"entries\": {";
     bool first = true;
     for (const auto& kv : entries) {
-        f << (first ? "\n" : ",\n") << "    \"" << kv.first << "\": {\"bxw\": " << kv.second.bxw
-          << ", \"bz\": " << kv.second.bz << ", \"ctas_per_sm\": " << kv.second.ctas_per_sm
-          << ", \"us\": " << kv.second.us << "}";
+        const Shape& sh = kv.second.shape;
+        f << (first ? "\n" : ",\n") << "    \"" << kv.first << "\": {\"kernel\": " << sh.kernel
+          << ", \"bxw\": " << sh.bxw << ", \"bz\": " << sh.bz << ", \"steps\": " << sh.steps
+          << ", \"ctas_per_sm\": " << sh.ctas_per_sm << ", \"us\": " << kv.second.us << "}";
         first = false;
     }
     f << "\n  }\n}\n";
@@ -76,14 +77,19 @@ bool TuneTable::load(const std::string& path) {
         if (k1 == std::string::npos || b0 == std::string::npos || b1 == std::string::npos) break;
         const std::string key = s.substr(k0 + 1, k1 - k0 - 1);
         const std::string body = s.substr(b0, b1 - b0 + 1);
-        double bxw = 0, bz = 0, cps = 0, us = 0;
+        double kernel = 1, bxw = 0, bz = 0, steps = 1, cps = 0, us = 0;
         if (field(body, "bxw", &bxw) && field(body, "bz", &bz)) {
+            field(body, "kernel", &kernel);
+            field(body, "steps", &steps);
             field(body, "ctas_per_sm", &cps);
             field(body, "us", &us);
             TuneEntry e;
-            e.bxw = (int)bxw;
-            e.bz = (int)bz;
-            e.ctas_per_sm = (int)cps;
+            e.shape.kernel = (int)kernel;
+            e.shape.bxw = (int)bxw;
+            e.shape.bz = (int)bz;
+            e.shape.steps = (int)steps;
+            e.shape.ctas_per_sm = (int)cps;
+            e.shape.finish();
             e.us = us;
             entries[key] = e;
         }
@@ -122,19 +128,37 @@ extern "C" hd_status hd_autotune(hd_context* ctx, const hd_pair_desc* pairs, int
     }
     repeats = std::max(1, repeats);
     std::vector<hd_result> res(n), ref(n);
-    const int shapes[][2] = {{2, 4}, {2, 8}, {2, 16}, {4, 4}, {4, 8}, {4, 16}, {8, 4}, {8, 8}, {8, 16}};
-    const int cps_list[] = {0, 1, 2};
+    // candidates: the one-step kernel over its brick shapes, the blocked
+    // kernel over steps per barrier and depth, each at two grid sizes
+    std::vector<Shape> cands;
+    for (int bxw : {2, 4, 8})
+        for (int bz : {4, 8, 16}) {
+            Shape c;
+            c.kernel = 1;
+            c.bxw = bxw;
+            c.bz = bz;
+            cands.push_back(c);
+        }
+    for (int steps : {1, 2})
+        for (int bz : {8, 16}) {
+            Shape c;
+            c.kernel = 2;
+            c.steps = steps;
+            c.bz = bz;
+            cands.push_back(c);
+        }
     TuneEntry best;
     best.us = 1e300;
     std::string rep;
     bool have_ref = false;
-    for (const auto& sh : shapes) {
-        for (int cps : cps_list) {
+    for (Shape c : cands) {
+        for (int cps : {0, 1}) {
+            c.ctas_per_sm = cps;
+            c.finish();
             RunOpts ro;
             ro.se = se;
-            ro.bxw = sh[0];
-            ro.bz = sh[1];
-            ro.ctas_per_sm = cps;
+            ro.force_shape = true;
+            ro.shape = c;
             hd_status st = run_pairs(ctx, in.data(), n, ctx->stream, ro, res.data());  // warm-up
             if (st != HD_OK && st != HD_EMPTY_MASK) return st;
             if (!have_ref) {
@@ -143,7 +167,8 @@ extern "C" hd_status hd_autotune(hd_context* ctx, const hd_pair_desc* pairs, int
             } else {
                 for (int i = 0; i < n; ++i)
                     if (res[i].hd != ref[i].hd || res[i].sum_ab != ref[i].sum_ab || res[i].sum_ba != ref[i].sum_ba)
-                        return set_error(ctx, HD_ERR_CUDA, "autotune: shape %dx%d gave a different result", sh[0], sh[1]);
+                        return set_error(ctx, HD_ERR_CUDA, "autotune: kernel %d shape %dx%dx%d gave a different result",
+                                         c.kernel, c.bxw, c.by, c.bz);
             }
             std::vector<double> t;
             for (int r = 0; r < repeats; ++r) {
@@ -155,14 +180,13 @@ extern "C" hd_status hd_autotune(hd_context* ctx, const hd_pair_desc* pairs, int
             }
             std::sort(t.begin(), t.end());
             const double med = t[t.size() / 2];
-            char line[128];
-            std::snprintf(line, sizeof line, "bxw=%d bz=%d cps=%d: %.1f us\n", sh[0], sh[1], cps, med);
+            char line[160];
+            std::snprintf(line, sizeof line, "kernel=%d bxw=%d by=%d bz=%d steps=%d cps=%d: %.1f us\n", c.kernel, c.bxw,
+                          c.by, c.bz, c.steps, cps, med);
             rep += line;
             if (med < best.us) {
                 best.us = med;
-                best.bxw = sh[0];
-                best.bz = sh[1];
-                best.ctas_per_sm = cps;
+                best.shape = c;
             }
         }
     }
@@ -172,8 +196,8 @@ extern "C" hd_status hd_autotune(hd_context* ctx, const hd_pair_desc* pairs, int
     const std::string key = tune_key(se, vox, n);
     ctx->tune.entries[key] = best;
     char line[160];
-    std::snprintf(line, sizeof line, "best %s: bxw=%d bz=%d cps=%d %.1f us\n", key.c_str(), best.bxw, best.bz,
-                  best.ctas_per_sm, best.us);
+    std::snprintf(line, sizeof line, "best %s: kernel=%d bxw=%d bz=%d steps=%d cps=%d %.1f us\n", key.c_str(),
+                  best.shape.kernel, best.shape.bxw, best.shape.bz, best.shape.steps, best.shape.ctas_per_sm, best.us);
     rep += line;
     if (!ctx->tuning_path.empty() && !ctx->tune.save(ctx->tuning_path))
         set_error(ctx, HD_OK, "autotune: could not write %s", ctx->tuning_path.c_str());

@@ -65,7 +65,8 @@ typedef enum hd_metric {
  * of d(a, B), hd_ab = max over a in A of d(a, B). */
 typedef struct hd_result {
     int32_t hd;          /* max(hd_ab, hd_ba); -1 when status != HD_OK */
-    int32_t iterations;  /* dilation steps run on the device (max over both directions) */
+    int32_t iterations;  /* grid-barrier iterations of the device loop for this call (each runs one
+                            or more dilation steps, see hd_options.kernel) */
     uint64_t sum_ab;
     uint64_t sum_ba;
     uint64_t n_a;
@@ -81,8 +82,8 @@ typedef struct hd_result {
 
 /* Options of a context.  Fill with hd_options_init, then override. */
 typedef struct hd_options {
-    int32_t brick_x_words;       /* brick width in 32-voxel words: 1,2,4,8; 0 = tuned */
-    int32_t brick_z;             /* brick depth in planes: 4, 8, 16; 0 = tuned */
+    int32_t brick_x_words;       /* kernel 1 brick width in 32-voxel words: 2, 4, 8; 0 = tuned */
+    int32_t brick_z;             /* brick depth in planes: 4, 8, 16 (kernel 1), 8, 16 (kernel 2); 0 = tuned */
     int32_t ctas_per_sm;         /* persistent CTAs per SM; 0 = occupancy maximum */
     int32_t max_iterations;      /* cap on dilation steps; 0 = W + H + D */
     int64_t barrier_timeout_ns;  /* give-up time of one grid-barrier wait; 0 = 10 s */
@@ -91,6 +92,11 @@ typedef struct hd_options {
                                     device can address them (default 1) */
     const char* tuning_table;    /* autotuner JSON table to load/store; NULL = none */
     int32_t record_timings;      /* record CUDA events around each kernel (hd_context_last_timings) */
+    int32_t kernel;              /* dilation kernel: 0 = tuned/default, 1 = one step per grid barrier
+                                    (brick_x_words x 32/brick_x_words rows x brick_z planes),
+                                    2 = temporally blocked (steps_per_barrier steps per barrier,
+                                    4 words x (32 - 2 steps) rows x brick_z planes) */
+    int32_t steps_per_barrier;   /* kernel 2: 1 or 2; 0 = tuned/default */
 } hd_options;
 
 /* Device durations of the last call's kernels (record_timings = 1), measured
@@ -100,9 +106,12 @@ typedef struct hd_timings {
     float setup_ms;      /* crop into job domains + first-step queue */
     float solve_ms;      /* persistent dilation loop */
     float total_ms;      /* first launch to last kernel end */
-    int32_t iterations;  /* dilation steps run by the persistent loop */
+    int32_t iterations;  /* grid-barrier iterations run by the persistent loop */
     int32_t grid_ctas;   /* CTAs of the persistent launch */
     int32_t brick_x_words, brick_z;
+    int32_t kernel;      /* 1 = one step per barrier, 2 = temporally blocked */
+    int32_t steps_per_barrier;
+    int32_t brick_rows;
 } hd_timings;
 
 typedef struct hd_context hd_context;

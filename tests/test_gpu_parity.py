@@ -115,9 +115,25 @@ def test_brick_shapes_agree(hd, oracle, metric):
     for bxw in (2, 4, 8):
         for bz in (4, 8, 16):
             for cps in (0, 1):
-                with hd.Context(0, brick_x_words=bxw, brick_z=bz, ctas_per_sm=cps) as c:
+                with hd.Context(0, kernel=1, brick_x_words=bxw, brick_z=bz, ctas_per_sm=cps) as c:
                     g = c.compute(da, db, metric)
-                assert_same(g, o, f"brick {bxw}x{bz} cps {cps}")
+                assert_same(g, o, f"one-step kernel brick {bxw}x{bz} cps {cps}")
+    for steps in (1, 2):
+        for bz in (8, 16):
+            for cps in (0, 1):
+                with hd.Context(0, kernel=2, steps_per_barrier=steps, brick_z=bz, ctas_per_sm=cps) as c:
+                    g = c.compute(da, db, metric)
+                assert_same(g, o, f"blocked kernel {steps} steps bz {bz} cps {cps}")
+
+
+@pytest.mark.parametrize("metric", ["se6", "se18"])
+@pytest.mark.parametrize("kernel,steps", [(1, 0), (2, 1), (2, 2)])
+def test_kernels_on_ragged_shapes(hd, oracle, metric, kernel, steps):
+    rng = np.random.default_rng(7)
+    with hd.Context(0, kernel=kernel, steps_per_barrier=steps) as c:
+        for shape in SHAPES:
+            a, b = random_pair(rng, shape, p_a=0.03, p_b=0.01)
+            assert_same(c.compute(cuda(a), cuda(b), metric), oracle.forbench(a, b, metric), f"{shape}")
 
 
 def test_shifted_union_midsize(ctx, oracle):
