@@ -218,7 +218,11 @@ hd_status decode_result(const hdk::PairInfo& I, const hdk::JobState& s0, const h
 }
 
 Shape pick_shape(hd_context* ctx, int se, const PairIn* pairs, int n) {
-    Shape sh;  // default: blocked kernel, 2 steps per barrier, 4 x 28 x 8 bricks
+    // built-in default (the autotuner's winners on GB300): the blocked kernel
+    // with 4 x (32 - 2 steps) x 8 bricks, 4 steps per barrier for a single
+    // pair (fewest barriers), 2 for batches (the work per barrier is large)
+    Shape sh;
+    sh.steps = n <= 1 ? 4 : 2;
     double vox = 0;
     for (int i = 0; i < n; ++i) vox += (double)pairs[i].W * pairs[i].H * pairs[i].D;
     vox /= std::max(1, n);
@@ -341,6 +345,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     char* dbase = (char*)ctx->arena.ptr;
     char* hbase = (char*)ctx->pinned.ptr;
     const int g0 = ctx->g_next;
+    long long pack_tiles = 0, setup_tiles = 0;
 
     // ---- host-side descriptors ------------------------------------------
     std::memset(hbase, 0, upload_bytes);
@@ -373,6 +378,10 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         Dd.kmax = q.kmax;
         Dd.job0 = 2 * i;
         Dd.info = (PairInfo*)(dbase + off_infos) + i;
+        Dd.tile0 = pack_tiles;
+        Dd.stile0 = setup_tiles;
+        pack_tiles += hdk::tiles_of(hdk::pack_words(P.W, P.H, P.D));
+        setup_tiles += hdk::tiles_of(hdk::domain_cap_words(P.W, P.H, P.D));
     }
 
     // ---- uploads ----------------------------------------------------------
@@ -401,13 +410,13 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     }
 
     // ---- pack, set-up -----------------------------------------------------
-    long long max_words = 0;
-    for (int i = 0; i < n; ++i) max_words = std::max(max_words, plan[i].full_words);
-    const int grid_x = (int)std::min<long long>(1024, std::max<long long>(1, (max_words + 2047) / 2048));
+    // one CTA per tile up to 8 per SM, then striding
+    const int grid_pack = (int)std::min<long long>(std::max(ctx->sm_count * 8, 1), pack_tiles);
+    const int grid_setup = (int)std::min<long long>(std::max(ctx->sm_count * 8, 1), setup_tiles);
     const PairDesc* ddesc = (const PairDesc*)(dbase + off_descs);
     const bool timing = ctx->opt.record_timings != 0 && ctx->ev[0] != nullptr;
     if (timing) cudaEventRecord(ctx->ev[0], s);
-    e = hdk::launch_pack(ddesc, n, grid_x, s);
+    e = hdk::launch_pack(ddesc, n, pack_tiles, grid_pack, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "pack launch");
     Ctl* dctl = (Ctl*)(dbase + off_ctl);
     Job* djobs = (Job*)(dbase + off_jobs);
@@ -416,7 +425,8 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
                                  (unsigned long long*)(dbase + off_q[1]),
                                  (unsigned long long*)(dbase + off_q[2])};
     if (timing) cudaEventRecord(ctx->ev[1], s);
-    e = hdk::launch_setup(ddesc, n, grid_x, djobs, dstates, dq[g0 % 3], dctl, g0, bxw, by, bz, stats ? 1 : 0, s);
+    e = hdk::launch_setup(ddesc, n, setup_tiles, grid_setup, djobs, dstates, dq[g0 % 3], dctl, g0, bxw, by, bz,
+                          stats ? 1 : 0, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "setup launch");
     if (ro.map_a || ro.map_b) {
         e = hdk::launch_map_init(ddesc, ro.map_a, ro.map_b,

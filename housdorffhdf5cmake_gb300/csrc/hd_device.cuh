@@ -49,7 +49,22 @@ struct PairDesc {
     unsigned long long* tcount[2];
     uint32_t epoch;                // queue-entry tag of this pair's jobs (slot reuse)
     uint32_t pad_;
+    long long tile0;               // first packing tile of this pair
+    long long stile0;              // first set-up tile of this pair
 };
+
+// Packing and set-up split every pair into tiles of kTileWords words; one
+// launch covers the tiles of all pairs.  Packing tiles cover the packed
+// volume (wxf * H * D words), set-up tiles the domain capacity (rows padded
+// to 4 words: roundup(wxf, 4) * H * D).
+constexpr long long kTileWords = 8192;
+__host__ __device__ __forceinline__ long long pack_words(int W, int H, int D) {
+    return (long long)((W + 31) / 32) * H * D;
+}
+__host__ __device__ __forceinline__ long long domain_cap_words(int W, int H, int D) {
+    return (long long)((((W + 31) / 32) + 3) & ~3) * H * D;
+}
+__host__ __device__ __forceinline__ long long tiles_of(long long words) { return (words + kTileWords - 1) / kTileWords; }
 
 // One direction of a pair, written by the set-up kernel.
 struct Job {

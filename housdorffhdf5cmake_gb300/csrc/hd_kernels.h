@@ -7,11 +7,13 @@
 
 namespace hdk {
 
-cudaError_t launch_pack(const PairDesc* d_descs, int npairs, int grid_x, cudaStream_t s);
-// Brick geometry: bxw words x by rows x bz planes (both kernel families).
-cudaError_t launch_setup(const PairDesc* d_descs, int npairs, int grid_x, Job* jobs, JobState* states,
-                         unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz, int stats,
-                         cudaStream_t s);
+// Packing and set-up run over `ntiles` tiles of kTileWords words (descs[i].tile0
+// = first tile of pair i, increasing) with `grid` CTAs.  Brick geometry:
+// bxw words x by rows x bz planes (both kernel families).
+cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, int grid, cudaStream_t s);
+cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int grid, Job* jobs,
+                         JobState* states, unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
+                         int stats, cudaStream_t s);
 cudaError_t launch_zero_i32(int32_t* p, long long n, cudaStream_t s);
 cudaError_t launch_map_init(const PairDesc* d_descs, int32_t* map_a, int32_t* map_b, long long n,
                             cudaStream_t s);
@@ -26,7 +28,7 @@ const void* solve_kernel_ptr_se18(int bxw, int bz);
 
 // The temporally blocked kernel (hd_solve_tb.cuh): `steps` dilation steps per
 // grid barrier, bricks of 4 words x (32 - 2 steps) rows x bz planes.
-// Compiled: steps in {1, 2}, bz in {8, 16}, both elements.
+// Compiled: steps 1, 2 with bz 8, 16; steps 3, 4 with bz 8; both elements.
 const void* solve_tb_kernel_ptr(int se, int steps, int bz);
 const void* solve_tb_kernel_ptr_se6(int steps, int bz);
 const void* solve_tb_kernel_ptr_se18(int steps, int bz);

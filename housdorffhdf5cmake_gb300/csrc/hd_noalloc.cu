@@ -114,6 +114,8 @@ __global__ void noalloc_prepare(unsigned char* base, Layout L, const uint8_t* a,
     P->kmax = L.kmax;
     P->job0 = 0;
     P->info = I;
+    P->tile0 = 0;
+    P->stile0 = 0;
 }
 
 // Device-side counterpart of the host result decoding: counts, sums, HD,
@@ -213,16 +215,18 @@ extern "C" hd_status hd_compute_u8_device_noalloc(const uint8_t* d_a, const uint
         e = cudaGetLastError();
     }
     const hdk::PairDesc* desc = (const hdk::PairDesc*)(base + L.desc);
-    const long long words = (long long)L.wxf * H * D;
-    const int grid_x = (int)std::min<long long>(1024, std::max<long long>(1, (words + 2047) / 2048));
-    if (e == cudaSuccess) e = hdk::launch_pack(desc, 1, grid_x, s);
+    const long long ptiles = hdk::tiles_of(hdk::pack_words(W, H, D));
+    const long long stiles = hdk::tiles_of(hdk::domain_cap_words(W, H, D));
+    const int cap_ctas = std::max(slot->sm_count * 8, 1);
+    if (e == cudaSuccess) e = hdk::launch_pack(desc, 1, ptiles, (int)std::min<long long>(cap_ctas, ptiles), s);
     hdk::Job* jobs = (hdk::Job*)(base + L.jobs);
     hdk::JobState* states = (hdk::JobState*)(base + L.states);
     hdk::Ctl* ctl = (hdk::Ctl*)(base + L.ctl);
     unsigned long long* q[3] = {(unsigned long long*)(base + L.queue[0]), (unsigned long long*)(base + L.queue[1]),
                                 (unsigned long long*)(base + L.queue[2])};
     if (e == cudaSuccess)
-        e = hdk::launch_setup(desc, 1, grid_x, jobs, states, q[g0 % 3], ctl, g0, kBxw, 32 / kBxw, kBz, 0, s);
+        e = hdk::launch_setup(desc, 1, stiles, (int)std::min<long long>(cap_ctas, stiles), jobs, states, q[g0 % 3], ctl,
+                              g0, kBxw, 32 / kBxw, kBz, 0, s);
     if (e == cudaSuccess) {
         hdk::SolveParams sp{};
         sp.jobs = jobs;

@@ -58,36 +58,24 @@ __device__ __forceinline__ int warp_max(int v) {
     return v;
 }
 
-// grid (X, npairs), block 256.  Thread per packed word of both masks.
-__global__ void __launch_bounds__(256) pack_kernel(const PairDesc* __restrict__ descs) {
-    const PairDesc& P = descs[blockIdx.y];
-    const int W = P.W, H = P.H, wxf = P.wxf;
-    const long long total = (long long)wxf * H * P.D;
-    const long long nbytes = (long long)W * H * P.D;
-    const bool aligned = P.aligned != 0;
+// The pair that owns work tile `tile` (first tiles increase with the pair
+// index; setup = false: packing tiles, true: set-up tiles).
+__device__ __forceinline__ int pair_of_tile(const PairDesc* __restrict__ descs, int npairs, long long tile,
+                                            bool setup) {
+    int lo = 0, hi = npairs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((setup ? descs[mid].stile0 : descs[mid].tile0) <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Bounding-box / count accumulation of one packed word pair.
+struct PackAcc {
     unsigned long long na = 0, nb = 0, nab = 0;
     int bb[6] = {INT_MAX, -1, INT_MAX, -1, INT_MAX, -1};
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        const long long r = t / wxf;
-        const int w = (int)(t - r * wxf);
-        const long long base = r * W + 32LL * w;
-        const long long ch = base >> 4;
-        const int off = (int)(base & 15);
-        const int nbits = min(32, W - 32 * w);
-        const uint32_t keep = nbits == 32 ? 0xffffffffu : ((1u << nbits) - 1u);
-        uint64_t va = chunk_bits(P.a, ch, nbytes, aligned) |
-                      ((uint64_t)chunk_bits(P.a, ch + 1, nbytes, aligned) << 16);
-        uint64_t vb = chunk_bits(P.b, ch, nbytes, aligned) |
-                      ((uint64_t)chunk_bits(P.b, ch + 1, nbytes, aligned) << 16);
-        if (off) {
-            va |= (uint64_t)chunk_bits(P.a, ch + 2, nbytes, aligned) << 32;
-            vb |= (uint64_t)chunk_bits(P.b, ch + 2, nbytes, aligned) << 32;
-        }
-        const uint32_t wa = (uint32_t)(va >> off) & keep;
-        const uint32_t wb = (uint32_t)(vb >> off) & keep;
-        P.pa[t] = wa;
-        P.pb[t] = wb;
+    __device__ __forceinline__ void add(uint32_t wa, uint32_t wb, long long r, int w, int H) {
         na += __popc(wa);
         nb += __popc(wb);
         nab += __popc(wa & wb);
@@ -102,13 +90,108 @@ __global__ void __launch_bounds__(256) pack_kernel(const PairDesc* __restrict__ 
             bb[5] = max(bb[5], z);
         }
     }
-    na = warp_sum_u64(na);
-    nb = warp_sum_u64(nb);
-    nab = warp_sum_u64(nab);
+};
+
+// 1D grid, block 256: CTAs stride over the tiles of all pairs (kTileWords
+// packed words per tile).
+//   fast path (rows of whole words, 16-byte aligned masks): word t covers bytes
+//   [32 t, 32 t + 32), read as two 16-byte chunks by two neighbouring lanes;
+//   general path: word by word, three 16-byte chunks around the word's bytes.
+__device__ __forceinline__ void flush_acc(const PairDesc& P, const PackAcc& acc);
+
+__device__ __forceinline__ void pack_tile(const PairDesc& P, long long tile_in_pair);
+
+__global__ void __launch_bounds__(256) pack_kernel(const PairDesc* __restrict__ descs, int npairs,
+                                                   long long ntiles) {
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int pi = pair_of_tile(descs, npairs, tile, false);
+        pack_tile(descs[pi], tile - descs[pi].tile0);
+    }
+}
+
+__device__ __forceinline__ void pack_tile(const PairDesc& P, long long tile_in_pair) {
+    const int W = P.W, H = P.H, wxf = P.wxf;
+    const long long total_all = (long long)wxf * H * P.D;
+    const long long nbytes = (long long)W * H * P.D;
+    const bool aligned = P.aligned != 0;
+    // this tile's words [w_lo, w_hi) of the pair
+    const long long w_lo = tile_in_pair * kTileWords;
+    const long long total = min(total_all, w_lo + kTileWords);
+    const long long tid = threadIdx.x;
+    const long long nthr = blockDim.x;
+    PackAcc acc;
+    if (aligned && (W & 31) == 0) {
+        // Coalesced: per load instruction the warp reads 32 consecutive
+        // 16-byte chunks (512 B); lane l's chunk holds 16 voxels, even lanes
+        // take the odd neighbour's 16 bits and own a word.  A warp handles 4 x
+        // 16 words of each mask per round, all 8 loads issued first.
+        const uint4* a4 = reinterpret_cast<const uint4*>(P.a);
+        const uint4* b4 = reinterpret_cast<const uint4*>(P.b);
+        const int lane = threadIdx.x & 31;
+        const long long warp = tid >> 5, nwarp = nthr >> 5;
+        const long long chunks = 2 * total;  // end of this tile in 16-byte chunks of one mask
+        for (long long c0 = 2 * w_lo + warp * 128; c0 < chunks; c0 += nwarp * 128) {
+            uint4 va[4], vb[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const long long c = c0 + i * 32 + lane;
+                if (c < chunks) {
+                    va[i] = a4[c];
+                    vb[i] = b4[c];
+                } else {
+                    va[i] = vb[i] = make_uint4(0u, 0u, 0u, 0u);
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const uint32_t la = nz16(va[i]), lb = nz16(vb[i]);
+                const uint32_t ha = __shfl_down_sync(0xffffffffu, la, 1);
+                const uint32_t hb = __shfl_down_sync(0xffffffffu, lb, 1);
+                const long long c = c0 + i * 32 + lane;
+                if ((lane & 1) == 0 && c < chunks) {
+                    const long long t = c >> 1;
+                    const uint32_t wa = la | (ha << 16), wb = lb | (hb << 16);
+                    P.pa[t] = wa;
+                    P.pb[t] = wb;
+                    const long long r = t / wxf;
+                    acc.add(wa, wb, r, (int)(t - r * wxf), H);
+                }
+            }
+        }
+    } else {
+        for (long long t = w_lo + tid; t < total; t += nthr) {
+            const long long r = t / wxf;
+            const int w = (int)(t - r * wxf);
+            const long long base = r * W + 32LL * w;
+            const long long ch = base >> 4;
+            const int off = (int)(base & 15);
+            const int nbits = min(32, W - 32 * w);
+            const uint32_t keep = nbits == 32 ? 0xffffffffu : ((1u << nbits) - 1u);
+            uint64_t va = chunk_bits(P.a, ch, nbytes, aligned) |
+                          ((uint64_t)chunk_bits(P.a, ch + 1, nbytes, aligned) << 16);
+            uint64_t vb = chunk_bits(P.b, ch, nbytes, aligned) |
+                          ((uint64_t)chunk_bits(P.b, ch + 1, nbytes, aligned) << 16);
+            if (off) {
+                va |= (uint64_t)chunk_bits(P.a, ch + 2, nbytes, aligned) << 32;
+                vb |= (uint64_t)chunk_bits(P.b, ch + 2, nbytes, aligned) << 32;
+            }
+            const uint32_t wa = (uint32_t)(va >> off) & keep;
+            const uint32_t wb = (uint32_t)(vb >> off) & keep;
+            P.pa[t] = wa;
+            P.pb[t] = wb;
+            acc.add(wa, wb, r, w, H);
+        }
+    }
+    flush_acc(P, acc);
+}
+
+__device__ __forceinline__ void flush_acc(const PairDesc& P, const PackAcc& acc) {
+    unsigned long long na = warp_sum_u64(acc.na), nb = warp_sum_u64(acc.nb), nab = warp_sum_u64(acc.nab);
+    int bb[6];
 #pragma unroll
     for (int i = 0; i < 6; i += 2) {
-        bb[i] = warp_min(bb[i]);
-        bb[i + 1] = warp_max(bb[i + 1]);
+        bb[i] = warp_min(acc.bb[i]);
+        bb[i + 1] = warp_max(acc.bb[i + 1]);
     }
     if ((threadIdx.x & 31) == 0) {
         PairInfo* I = P.info;
@@ -158,21 +241,39 @@ __device__ __forceinline__ Domain make_domain(const PairDesc& P, const PairInfo&
     return m;
 }
 
-// grid (X, npairs), block 256.
-__global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__ descs, Job* jobs,
-                                                    JobState* states, unsigned long long* queue0,
+__device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_pair, Job* jobs, JobState* states,
+                                           unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz);
+
+// 1D grid, block 256: CTAs stride over the tiles of all pairs; tile 0 of a
+// pair also writes its job descriptors.  A pair's tiles cover its full
+// volume's word count, an upper bound of its domain.
+__global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__ descs, int npairs, long long ntiles,
+                                                    Job* jobs, JobState* states, unsigned long long* queue0,
                                                     Ctl* ctl, int g0, int bxw, int by, int bz, int stats) {
-    const PairDesc& P = descs[blockIdx.y];
+    (void)stats;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int pi = pair_of_tile(descs, npairs, tile, true);
+        setup_tile(descs[pi], tile - descs[pi].stile0, jobs, states, queue0, ctl, g0, bxw, by, bz);
+    }
+}
+
+__device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_pair, Job* jobs, JobState* states,
+                                           unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz) {
     const PairInfo I = *P.info;
     const bool empty_a = I.n_a == 0, empty_b = I.n_b == 0;
     const unsigned long long rem[2] = {I.n_b - I.n_ab, I.n_a - I.n_ab};
-    const long long tid0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long nthr = (long long)gridDim.x * blockDim.x;
+    const long long cap = domain_cap_words(P.W, P.H, P.D);  // this pair's tiles cover [0, cap) words
+    const long long ntiles_pair = tiles_of(cap);
+    const long long w_lo = tile_in_pair * kTileWords, w_hi = min(cap, w_lo + kTileWords);
+    const long long tid0 = threadIdx.x;
+    const long long nthr = blockDim.x;
+    const bool first = tile_in_pair == 0;
     const int kmax = P.kmax;
     // histograms are zeroed for every pair
-    for (long long t = tid0; t < 2LL * (kmax + 1); t += nthr) P.hist[t / (kmax + 1)][t % (kmax + 1)] = 0ull;
+    if (first)
+        for (long long t = tid0; t < 2LL * (kmax + 1); t += nthr) P.hist[t / (kmax + 1)][t % (kmax + 1)] = 0ull;
     if (empty_a || empty_b) {
-        if (tid0 == 0) {
+        if (first && tid0 == 0) {
             for (int j = 0; j < 2; ++j) {
                 JobState& s = states[P.job0 + j];
                 s.sum = 0; s.remaining = 0; s.bricks = 0; s.hd = 0; s.last_k = 0;
@@ -188,7 +289,7 @@ __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__
     const Domain m = make_domain(P, I);
     const int nbx = (m.wx + bxw - 1) / bxw, nby = (m.h + by - 1) / by, nbz = (m.d + bz - 1) / bz;
     const long long nbricks = (long long)nbx * nby * nbz;
-    if (tid0 == 0) {
+    if (first && tid0 == 0) {
         for (int j = 0; j < 2; ++j) {
             Job& J = jobs[P.job0 + j];
             J.buf[0] = P.jb[j][0];
@@ -215,9 +316,9 @@ __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__
         }
     }
     // Crop copy.  Job 0 dilates A and must cover B; job 1 dilates B and covers A.
-    const long long words = (long long)m.pitch * m.h * m.d;
+    const long long words = min((long long)m.pitch * m.h * m.d, w_hi);
     const bool act0 = rem[0] > 0, act1 = rem[1] > 0;
-    for (long long t = tid0; t < words; t += nthr) {
+    for (long long t = w_lo + tid0; t < words; t += nthr) {
         const long long r = t / m.pitch;
         const int w = (int)(t - r * m.pitch);
         uint32_t a = 0, b = 0;
@@ -232,13 +333,16 @@ __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__
     }
     // First step of each active job: every brick of its domain (one
     // warp-aggregated append per 32 bricks).
+    // the bricks are split evenly over the pair's tiles
     const int lane = threadIdx.x & 31;
     const long long gwarp = tid0 >> 5, nwarps = nthr >> 5;
+    const long long b_per = (nbricks + ntiles_pair - 1) / ntiles_pair;
+    const long long b_lo = tile_in_pair * b_per, b_hi = min(nbricks, b_lo + b_per);
     for (int j = 0; j < 2; ++j) {
         if (!(j == 0 ? act0 : act1)) continue;
-        for (long long b0 = gwarp * 32; b0 < nbricks; b0 += nwarps * 32) {
+        for (long long b0 = b_lo + gwarp * 32; b0 < b_hi; b0 += nwarps * 32) {
             const long long t = b0 + lane;
-            const bool have = t < nbricks;
+            const bool have = t < b_hi;
             const unsigned mball = __ballot_sync(0xffffffffu, have);
             unsigned base = 0;
             if (lane == 0) base = atomicAdd(&ctl->qcount[g0 % 3], (unsigned)__popc(mball));
@@ -248,7 +352,6 @@ __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__
                     make_entry(P.epoch, (uint32_t)(P.job0 + j), (uint32_t)t);
         }
     }
-    (void)stats;
 }
 
 // Instrumented runs: zero the per-tile stamps and per-step tile counters.
@@ -276,17 +379,15 @@ __global__ void map_init_kernel(const PairDesc* __restrict__ descs, int32_t* map
 // ---- launch wrappers (called from the host orchestration) -----------------
 namespace hdk {
 
-cudaError_t launch_pack(const PairDesc* d_descs, int npairs, int grid_x, cudaStream_t s) {
-    dim3 grid(grid_x, npairs);
-    pack_kernel<<<grid, 256, 0, s>>>(d_descs);
+cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, int grid, cudaStream_t s) {
+    pack_kernel<<<grid, 256, 0, s>>>(d_descs, npairs, ntiles);
     return cudaGetLastError();
 }
 
-cudaError_t launch_setup(const PairDesc* d_descs, int npairs, int grid_x, Job* jobs, JobState* states,
-                         unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz, int stats,
-                         cudaStream_t s) {
-    dim3 grid(grid_x, npairs);
-    setup_kernel<<<grid, 256, 0, s>>>(d_descs, jobs, states, queue0, ctl, g0, bxw, by, bz, stats);
+cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int grid, Job* jobs,
+                         JobState* states, unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
+                         int stats, cudaStream_t s) {
+    setup_kernel<<<grid, 256, 0, s>>>(d_descs, npairs, ntiles, jobs, states, queue0, ctl, g0, bxw, by, bz, stats);
     return cudaGetLastError();
 }
 

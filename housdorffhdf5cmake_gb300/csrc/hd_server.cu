@@ -220,6 +220,7 @@ void tick(hd_server* s) {
     std::vector<void*> transient(admit.size(), nullptr);
     std::vector<PairDesc> descs;
     std::vector<Request*> admitted;
+    long long ptiles = 0, stiles = 0;
     for (size_t i = 0; i < admit.size(); ++i) {
         Request* r = admit[i];
         void* res = nullptr;
@@ -272,6 +273,10 @@ void tick(hd_server* s) {
         d.kmax = r->kmax;
         d.job0 = 2 * r->slot;
         d.epoch = ++s->slot_epoch[r->slot];
+        d.tile0 = ptiles;
+        d.stile0 = stiles;
+        ptiles += hdk::tiles_of(hdk::pack_words(r->W, r->H, r->D));
+        stiles += hdk::tiles_of(hdk::domain_cap_words(r->W, r->H, r->D));
         d.info = (PairInfo*)(rb + r->off_info);
         descs.push_back(d);
         admitted.push_back(r);
@@ -289,12 +294,12 @@ void tick(hd_server* s) {
         e = cudaMemcpyAsync(s->d_descs, hp, sizeof(PairDesc) * descs.size(), cudaMemcpyHostToDevice, st);
         for (size_t i = 0; i < admitted.size() && e == cudaSuccess; ++i)
             e = cudaMemcpyAsync(descs[i].info, &init[i], sizeof(PairInfo), cudaMemcpyHostToDevice, st);
-        long long max_words = 0;
-        for (auto* r : admitted) max_words = std::max(max_words, (long long)r->wxf * r->H * r->D);
-        const int gx = (int)std::min<long long>(1024, std::max<long long>(1, (max_words + 2047) / 2048));
-        if (e == cudaSuccess) e = hdk::launch_pack(s->d_descs, (int)admitted.size(), gx, st);
+        const int cap_ctas = std::max(s->ctx->sm_count * 8, 1);
         if (e == cudaSuccess)
-            e = hdk::launch_setup(s->d_descs, (int)admitted.size(), gx, s->d_jobs, s->d_states,
+            e = hdk::launch_pack(s->d_descs, (int)admitted.size(), ptiles, (int)std::min<long long>(cap_ctas, ptiles), st);
+        if (e == cudaSuccess)
+            e = hdk::launch_setup(s->d_descs, (int)admitted.size(), stiles, (int)std::min<long long>(cap_ctas, stiles),
+                                  s->d_jobs, s->d_states,
                                   s->d_queue[s->g_next % 3], s->d_ctl, s->g_next, s->shape.bxw, s->shape.by,
                                   s->shape.bz, 0, st);
         // pageable sources of cudaMemcpyAsync and the info initialisers must
@@ -502,7 +507,7 @@ hd_status hd_server_create(hd_context* ctx, const hd_server_options* opt, hd_ser
             return HD_ERR_CUDA;
         }
         PairIn typical{nullptr, nullptr, 256, 256, 160, nullptr, nullptr};
-        s->shape = pick_shape(ctx, s->se, &typical, 16);
+        s->shape = pick_shape(ctx, s->se, &typical, 16);  // a batch-like mix of pairs
         const int cps = s->shape.ctas_per_sm;
         s->solve_fn = solve_fn_of(s->se, s->shape);
         if (!s->solve_fn) {

@@ -21,9 +21,10 @@
 // step k_base + s, the distance of those voxels) and the final level is
 // written to the other ping-pong buffer.
 //
-// Frontier rule: a brick is queued for the next iteration iff its state or
-// the part of a neighbour within reach of its halo (the adjacent word in x,
-// T rows / planes in y / z) changed during this iteration.  A brick not
+// Frontier rule: a brick is queued for the next iteration iff its state, or a
+// neighbour's state within T voxels of their shared face, changed during this
+// iteration (T steps reach no further; for edge and corner neighbours the
+// flags of all the faces involved must be set).  A brick not
 // queued has D^{(i+1)T} = D^{iT} on itself and its halo, so its next T steps
 // change nothing and both ping-pong buffers already hold its state.
 #pragma once
@@ -53,55 +54,65 @@ __device__ __forceinline__ void cp_async_wait_all() {
     asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
-template <int T, int BZ, bool SE18>
-__device__ __forceinline__ void brick_tb(const SolveParams& p, int jid, unsigned lb, unsigned epoch, int g,
-                                         unsigned char* wsm) {
+// One queue item of the blocked kernel, decoded and with its copies issued.
+struct TbItem {
+    const Job* Jp;
+    JobState* st;
+    int jid;
+    unsigned epoch;
+    unsigned lb;
+    int iter, kb;
+    int bx, by, bz;
+    bool live;
+};
+
+// Decodes a queue entry, checks that its job still needs work, and issues
+// every copy of the brick into the warp's shared memory (rows, planes and
+// halo words outside the domain are zero-filled).  No wait.
+template <int T, int BZ>
+__device__ __forceinline__ void tb_issue(const SolveParams& p, unsigned long long e, int g, unsigned char* wsm,
+                                         TbItem& it) {
     constexpr int IW = 4;
-    constexpr int NW = IW + 2;
     constexpr int BYI = 32 - 2 * T;
     constexpr int NP = BZ + 2 * T;
     using SM = TbSmem<T, BZ>;
     const int lane = threadIdx.x & 31;
-    JobState* st = p.states + jid;
-    if (ld_relaxed_s32(&st->active) == 0) return;
-    const Job* Jp = p.jobs + jid;
-    if ((Jp->epoch & 0xffu) != epoch) return;
-    const int iter = g - Jp->k0;  // this job's iteration index, 0-based
-    const int kb = iter * T;      // steps completed before this iteration
-    if (kb + 1 > Jp->kmax) {
+    it.jid = (int)((e >> 32) & 0xffffffu);
+    it.lb = (unsigned)e;
+    it.epoch = (unsigned)(e >> 56);
+    it.st = p.states + it.jid;
+    it.Jp = p.jobs + it.jid;
+    it.live = false;
+    if (ld_relaxed_s32(&it.st->active) == 0) return;     // nothing left to cover
+    const Job* Jp = it.Jp;
+    if ((Jp->epoch & 0xffu) != it.epoch) return;         // left over from the slot's previous pair
+    it.iter = g - Jp->k0;
+    it.kb = it.iter * T;
+    if (it.kb + 1 > Jp->kmax) {
         if (lane == 0) {
-            st->status = kErrIterLimit;
+            it.st->status = kErrIterLimit;
             atomicCAS(&p.ctl->err, 0, kErrIterLimit);
         }
         return;
     }
-    const int nbx = Jp->nbx, nby = Jp->nby, nbz = Jp->nbz;
+    const int nbx = Jp->nbx, nby = Jp->nby;
+    it.bx = (int)(it.lb % (unsigned)nbx);
+    const unsigned tq = it.lb / (unsigned)nbx;
+    it.by = (int)(tq % (unsigned)nby);
+    it.bz = (int)(tq / (unsigned)nby);
+    it.live = true;
     const int Wx = Jp->wx, Hd = Jp->h, Dd = Jp->d;
-    const int bx = (int)(lb % (unsigned)nbx);
-    const unsigned tq = lb / (unsigned)nbx;
-    const int by = (int)(tq % (unsigned)nby);
-    const int bz = (int)(tq / (unsigned)nby);
-    const int wx0 = bx * IW, y0 = by * BYI, z0 = bz * BZ;
-    const int y = y0 - T + lane;
+    const int wx0 = it.bx * IW, z0 = it.bz * BZ;
+    const int y = it.by * BYI - T + lane;
     const bool rowv = y >= 0 && y < Hd;
     const bool inter = rowv && lane >= T && lane < 32 - T;
-    const uint32_t* __restrict__ src = Jp->buf[iter & 1];
-    uint32_t* __restrict__ dst = Jp->buf[(iter + 1) & 1];
-    uint32_t* __restrict__ U = Jp->U;
+    const uint32_t* src = Jp->buf[it.iter & 1];
+    const uint32_t* U = Jp->U;
     const int pitch = Jp->pitch;
     const int plane = pitch * Hd;
     const int rowoff = (rowv ? y : 0) * pitch + wx0;
     const bool hl_ok = rowv && wx0 > 0;
     const bool hr_ok = rowv && wx0 + IW < Wx;
-    uint32_t wm[NW];  // valid bits of each word of this lane's row
-#pragma unroll
-    for (int j = 0; j < NW; ++j) {
-        const int w = wx0 - 1 + j;
-        wm[j] = (rowv && w >= 0 && w < Wx) ? (w == Wx - 1 ? Jp->tailmask : kFull) : 0u;
-    }
-
-    // Stage this lane's rows: every copy of the brick is in flight at once;
-    // rows, planes and halo words outside the domain are zero-filled.
     const uint32_t s_in = (uint32_t)__cvta_generic_to_shared(wsm);
     const uint32_t s_u = s_in + SM::kInBytes;
 #pragma unroll
@@ -121,7 +132,46 @@ __device__ __forceinline__ void brick_tb(const SolveParams& p, int jid, unsigned
         cp_async16(s_u + (uint32_t)((i * 32 + lane) * SM::kURowBytes), U + (ok ? z * plane + rowoff : 0),
                    ok ? 16u : 0u);
     }
-    cp_async_wait_all();  // each lane reads back only its own rows
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// What the epilogue of an item needs from its compute phase.
+constexpr int kTbMaxSteps = 4;
+struct TbOut {
+    unsigned cnt[kTbMaxSteps];  // newly covered voxels per step of the item
+    bool any, fxl, fxh, fyl, fyh, fzl, fzh;
+};
+
+// Waits for the item's copies, runs its T steps and writes its state and
+// uncovered-target words back.
+template <int T, int BZ, bool SE18>
+__device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& it, unsigned char* wsm, TbOut& res) {
+    static_assert(T >= 1 && T <= kTbMaxSteps, "steps per barrier out of range");
+    constexpr int IW = 4;
+    constexpr int NW = IW + 2;
+    constexpr int BYI = 32 - 2 * T;
+    constexpr int NP = BZ + 2 * T;
+    using SM = TbSmem<T, BZ>;
+    const int lane = threadIdx.x & 31;
+    const Job* Jp = it.Jp;
+    const int Wx = Jp->wx, Hd = Jp->h, Dd = Jp->d;
+    const int wx0 = it.bx * IW, z0 = it.bz * BZ;
+    const int y = it.by * BYI - T + lane;
+    const bool rowv = y >= 0 && y < Hd;
+    const bool inter = rowv && lane >= T && lane < 32 - T;
+    uint32_t* __restrict__ dst = Jp->buf[(it.iter + 1) & 1];
+    uint32_t* __restrict__ U = Jp->U;
+    const int pitch = Jp->pitch;
+    const int plane = pitch * Hd;
+    const int rowoff = (rowv ? y : 0) * pitch + wx0;
+    const int kb = it.kb;
+    uint32_t wm[NW];  // valid bits of each word of this lane's row
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+        const int w = wx0 - 1 + j;
+        wm[j] = (rowv && w >= 0 && w < Wx) ? (w == Wx - 1 ? Jp->tailmask : kFull) : 0u;
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");  // each lane reads back only its own rows
 
     auto plane_ok = [&](int r) {  // streamed plane index r -> inside the domain
         const int z = z0 - T + r;
@@ -182,6 +232,7 @@ __device__ __forceinline__ void brick_tb(const SolveParams& p, int jid, unsigned
     uint32_t d_any = 0, d_xl = 0, d_xh = 0, d_zl = 0, d_zh = 0, u_hits = 0;
     const bool band_yl = inter && (lane - T) < T;
     const bool band_yh = inter && (lane - T) >= BYI - T;
+    (void)p;
 
 #pragma unroll
     for (int q = 0; q < NP; ++q) {
@@ -229,11 +280,14 @@ __device__ __forceinline__ void brick_tb(const SolveParams& p, int jid, unsigned
                         const uint4 c0 = *reinterpret_cast<const uint4*>(in_row(r));
                         const uint32_t dx0 = out[1] ^ (c0.x & wm[1]), dx3 = out[4] ^ (c0.w & wm[4]);
                         const uint32_t dall = dx0 | (out[2] ^ (c0.y & wm[2])) | (out[3] ^ (c0.z & wm[3])) | dx3;
+                        // only changes within T voxels of an x face can reach
+                        // the x neighbour's interior during its next T steps
+                        constexpr uint32_t kLoBits = (1u << T) - 1u, kHiBits = ~(0xffffffffu >> T);
                         if (u_hits & (1u << (r - T)))
                             *reinterpret_cast<uint4*>(U + off) = *reinterpret_cast<const uint4*>(u_row(r - T));
                         d_any |= dall;
-                        d_xl |= dx0;
-                        d_xh |= dx3;
+                        d_xl |= dx0 & kLoBits;
+                        d_xh |= dx3 & kHiBits;
                         if (r - T < T) d_zl |= dall;
                         if (r - T >= BZ - T) d_zh |= dall;
                     }
@@ -242,71 +296,79 @@ __device__ __forceinline__ void brick_tb(const SolveParams& p, int jid, unsigned
         }
     }
 
-    // per-step hit counts
+    // per-step hit counts and frontier flags
 #pragma unroll
     for (int s = 0; s < T; ++s) {
         unsigned c = cnt[s];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
-        cnt[s] = c;
+        res.cnt[s] = c;
     }
+    res.any = __any_sync(kFull, d_any != 0);
+    res.fxl = __any_sync(kFull, d_xl != 0);
+    res.fxh = __any_sync(kFull, d_xh != 0);
+    res.fyl = __any_sync(kFull, band_yl && d_any != 0);
+    res.fyh = __any_sync(kFull, band_yh && d_any != 0);
+    res.fzl = __any_sync(kFull, d_zl != 0);
+    res.fzh = __any_sync(kFull, d_zh != 0);
+}
+
+// Counts, frontier, completion.  The completion atomic's return value is
+// consumed last, so its latency overlaps the frontier atomics.
+template <int T, bool SE18>
+__device__ __forceinline__ void tb_epilogue(const SolveParams& p, const TbItem& it, const TbOut& res, int g) {
+    const int lane = threadIdx.x & 31;
+    const Job* Jp = it.Jp;
+    JobState* st = it.st;
+    unsigned long long tot = 0, left = ~0ull;
     if (lane == 0) {
-        unsigned long long tot = 0;
 #pragma unroll
         for (int s = 0; s < T; ++s) {
-            if (cnt[s]) {
-                const int k = kb + s + 1;
-                tot += cnt[s];
-                atomicAdd(&st->sum, (unsigned long long)k * cnt[s]);
+            if (res.cnt[s]) {
+                const int k = it.kb + s + 1;
+                tot += res.cnt[s];
+                atomicAdd(&st->sum, (unsigned long long)k * res.cnt[s]);
                 atomicMax(&st->hd, k);
-                atomicAdd(&Jp->hist[k], (unsigned long long)cnt[s]);
+                atomicAdd(&Jp->hist[k], (unsigned long long)res.cnt[s]);
             }
         }
-        if (tot) {
-            const unsigned long long left = atomicAdd(&st->remaining, (unsigned long long)(-(long long)tot));
-            if (left == tot) {
-                st->active = 0;
-                atomicSub(&p.ctl->jobs_active, 1);
-            }
-        }
+        if (tot) left = atomicAdd(&st->remaining, (unsigned long long)(-(long long)tot));
         if (p.stats) atomicAdd(&st->bricks, 1ull);
     }
-
-    // frontier
-    if (!__any_sync(kFull, d_any != 0)) return;
-    const bool fxl = __any_sync(kFull, d_xl != 0);
-    const bool fxh = __any_sync(kFull, d_xh != 0);
-    const bool fyl = __any_sync(kFull, band_yl && d_any != 0);
-    const bool fyh = __any_sync(kFull, band_yh && d_any != 0);
-    const bool fzl = __any_sync(kFull, d_zl != 0);
-    const bool fzh = __any_sync(kFull, d_zh != 0);
-    bool need = false;
-    unsigned nlb = 0;
-    if (lane < 27) {
-        const int ox = lane % 3 - 1, oy = (lane / 3) % 3 - 1, oz = lane / 9 - 1;
-        const int nnz = (ox != 0) + (oy != 0) + (oz != 0);
-        need = SE18 || T > 1 || nnz <= 1;
-        if (ox < 0) need = need && fxl;
-        if (ox > 0) need = need && fxh;
-        if (oy < 0) need = need && fyl;
-        if (oy > 0) need = need && fyh;
-        if (oz < 0) need = need && fzl;
-        if (oz > 0) need = need && fzh;
-        const int nx = bx + ox, ny = by + oy, nz = bz + oz;
-        need = need && nx >= 0 && nx < nbx && ny >= 0 && ny < nby && nz >= 0 && nz < nbz;
-        if (need) {
-            nlb = (unsigned)((nz * nby + ny) * nbx + nx);
-            need = atomicMax(&p.stamps[Jp->brick0 + nlb], g + 1) < g + 1;
+    if (res.any) {
+        const int nbx = Jp->nbx, nby = Jp->nby, nbz = Jp->nbz;
+        bool need = false;
+        unsigned nlb = 0;
+        if (lane < 27) {
+            const int ox = lane % 3 - 1, oy = (lane / 3) % 3 - 1, oz = lane / 9 - 1;
+            const int nnz = (ox != 0) + (oy != 0) + (oz != 0);
+            need = SE18 || T > 1 || nnz <= 1;
+            if (ox < 0) need = need && res.fxl;
+            if (ox > 0) need = need && res.fxh;
+            if (oy < 0) need = need && res.fyl;
+            if (oy > 0) need = need && res.fyh;
+            if (oz < 0) need = need && res.fzl;
+            if (oz > 0) need = need && res.fzh;
+            const int nx = it.bx + ox, ny = it.by + oy, nz = it.bz + oz;
+            need = need && nx >= 0 && nx < nbx && ny >= 0 && ny < nby && nz >= 0 && nz < nbz;
+            if (need) {
+                nlb = (unsigned)((nz * nby + ny) * nbx + nx);
+                need = atomicMax(&p.stamps[Jp->brick0 + nlb], g + 1) < g + 1;
+            }
+        }
+        const unsigned m = __ballot_sync(kFull, need);
+        if (m) {
+            const int qn = (g + 1) % 3;
+            unsigned long long* qdst = qn == 0 ? p.queue[0] : (qn == 1 ? p.queue[1] : p.queue[2]);
+            unsigned base = 0;
+            if (lane == 0) base = atomicAdd(&p.ctl->qcount[qn], (unsigned)__popc(m));
+            base = __shfl_sync(kFull, base, 0);
+            if (need) qdst[base + __popc(m & ((1u << lane) - 1u))] = make_entry(it.epoch, (uint32_t)it.jid, nlb);
         }
     }
-    const unsigned m = __ballot_sync(kFull, need);
-    if (m) {
-        const int qn = (g + 1) % 3;
-        unsigned long long* qdst = qn == 0 ? p.queue[0] : (qn == 1 ? p.queue[1] : p.queue[2]);
-        unsigned base = 0;
-        if (lane == 0) base = atomicAdd(&p.ctl->qcount[qn], (unsigned)__popc(m));
-        base = __shfl_sync(kFull, base, 0);
-        if (need) qdst[base + __popc(m & ((1u << lane) - 1u))] = make_entry(epoch, (uint32_t)jid, nlb);
+    if (lane == 0 && tot && left == tot) {  // this brick covered the job's last target voxel
+        st->active = 0;
+        atomicSub(&p.ctl->jobs_active, 1);
     }
 }
 
@@ -330,14 +392,28 @@ __global__ void __launch_bounds__(kTbWarps * 32) solve_tb_kernel(SolveParams p) 
     const unsigned nw = gridDim.x * wpb;
     int g = p.g0;
     int it = 0;
+    unsigned char* wsm = tb_smem + (threadIdx.x >> 5) * TbSmem<T, BZ>::kWarpBytes;
     if (cnt > 0) {
         for (;;) {
             const int qi = g % 3;
             const unsigned long long* Q = qi == 0 ? p.queue[0] : (qi == 1 ? p.queue[1] : p.queue[2]);
-            for (unsigned i = gw; i < cnt; i += nw) {
-                const unsigned long long e = Q[i];
-                brick_tb<T, BZ, SE18>(p, (int)((e >> 32) & 0xffffffu), (unsigned)e, (unsigned)(e >> 56), g,
-                                      tb_smem + (threadIdx.x >> 5) * TbSmem<T, BZ>::kWarpBytes);
+            // two-stage pipeline per warp: the next brick's copies are in
+            // flight while this brick's epilogue atomics run
+            TbItem cur;
+            cur.live = false;
+            unsigned i = gw;
+            if (i < cnt) tb_issue<T, BZ>(p, Q[i], g, wsm, cur);
+            while (i < cnt) {
+                const unsigned in = i + nw;
+                const unsigned long long en = in < cnt ? Q[in] : 0ull;
+                TbOut res;
+                if (cur.live) tb_compute<T, BZ, SE18>(p, cur, wsm, res);
+                TbItem nxt;
+                nxt.live = false;
+                if (in < cnt) tb_issue<T, BZ>(p, en, g, wsm, nxt);
+                if (cur.live) tb_epilogue<T, SE18>(p, cur, res, g);
+                cur = nxt;
+                i = in;
             }
             const bool cont = grid_step_barrier(ctl, gen, g, p.timeout_ns, &s_flag);
             ++g;
