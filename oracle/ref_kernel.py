@@ -2,14 +2,20 @@
 
 build() compiles, when the reference sources are present (this container),
 forBench/HausdorffDistance.cu from where it lies under /root/reference to PTX
-(oracle/_ref/forbench_dilate.ptx, the shipped macros: IS_3D 1, CHEBYSHEV 1 =
-the 18-neighbour element), and on any machine with nvcc the driver-API
-harness oracle/ref_kernel.cpp into oracle/_build/libref_kernel.so.  The PTX
-is text and travels with the repository snapshot to the GPU machine, where
-the driver compiles it for the GPU at load time.  Nothing of the reference is
-copied into the repository; oracle/_ref is git-ignored.
+twice, once per structuring element the reference's switches select
+(forBench/HausdorffDistance.cuh:7-8):
+  oracle/_ref/forbench_se18.ptx  as shipped: IS_3D 1, CHEBYSHEV 1
+  oracle/_ref/forbench_se6.ptx   CHEBYSHEV 0: a forced include first includes
+                                 the reference header (it is `#pragma once`,
+                                 so the .cu's own include of it is skipped)
+                                 and then redefines the macro to 0
+and, on any machine with nvcc, the driver-API harness oracle/ref_kernel.cpp
+into oracle/_build/libref_kernel.so.  The PTX is text and travels with the
+repository snapshot to the GPU machine, where the driver compiles it for the
+GPU at load time.  Nothing of the reference is copied into the repository;
+oracle/_ref is git-ignored.
 
-ref_hd(a, b) then runs the reference kernel under the host loop of
+ref_hd(a, b, se) then runs the reference kernel under the host loop of
 forBench/HausdorffDistance.cu:146-172 and returns its HD.
 """
 from __future__ import annotations
@@ -22,8 +28,10 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = "/root/reference/forBench/HausdorffDistance.cu"
-PTX = os.path.join(HERE, "_ref", "forbench_dilate.ptx")
+REF_DIR = "/root/reference/forBench"
+REF_SRC = os.path.join(REF_DIR, "HausdorffDistance.cu")
+PTX = {"se18": os.path.join(HERE, "_ref", "forbench_se18.ptx"),
+       "se6": os.path.join(HERE, "_ref", "forbench_se6.ptx")}
 HARNESS_SRC = os.path.join(HERE, "ref_kernel.cpp")
 HARNESS = os.path.join(HERE, "_build", "libref_kernel.so")
 
@@ -36,12 +44,23 @@ def _cuda_home():
 
 
 def build() -> None:
-    os.makedirs(os.path.dirname(PTX), exist_ok=True)
+    refdir = os.path.join(HERE, "_ref")
+    os.makedirs(refdir, exist_ok=True)
     os.makedirs(os.path.dirname(HARNESS), exist_ok=True)
-    if os.path.exists(REF_SRC) and (not os.path.exists(PTX) or os.path.getmtime(PTX) < os.path.getmtime(REF_SRC)):
-        tmp = PTX + f".tmp{os.getpid()}"
-        subprocess.run(["nvcc", "-ptx", "-arch=compute_103a", "-O3", "-w", "-o", tmp, REF_SRC], check=True)
-        os.replace(tmp, PTX)
+    if os.path.exists(REF_SRC):
+        for se, out in PTX.items():
+            if os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(REF_SRC):
+                continue
+            cmd = ["nvcc", "-ptx", "-arch=compute_103a", "-O3", "-w"]
+            if se == "se6":
+                force = os.path.join(refdir, "chebyshev0.h")
+                with open(force, "w") as f:
+                    f.write(f'#include "{os.path.join(REF_DIR, "HausdorffDistance.cuh")}"\n'
+                            "#undef CHEBYSHEV\n#define CHEBYSHEV 0\n")
+                cmd += ["-include", force]
+            tmp = out + f".tmp{os.getpid()}"
+            subprocess.run(cmd + ["-o", tmp, REF_SRC], check=True)
+            os.replace(tmp, out)
     home = _cuda_home()
     inc = os.path.join(home, "include")
     if not os.path.exists(HARNESS) or os.path.getmtime(HARNESS) < os.path.getmtime(HARNESS_SRC):
@@ -54,8 +73,8 @@ def build() -> None:
         os.replace(tmp, HARNESS)
 
 
-def available() -> bool:
-    return os.path.exists(PTX)
+def available(se: str = "se18") -> bool:
+    return os.path.exists(PTX[se])
 
 
 def _load():
@@ -70,15 +89,17 @@ def _load():
     return _lib
 
 
-def ref_hd(a, b, max_trips: int | None = None) -> int:
-    """HD of the reference's own kernel (18-neighbour element) on (D, H, W) masks."""
+def ref_hd(a, b, se: str = "se18", max_trips: int | None = None) -> int:
+    """HD of the reference's own kernel on (D, H, W) masks; se = "se18" (the
+    shipped CHEBYSHEV 1) or "se6" (CHEBYSHEV 0)."""
     a = np.ascontiguousarray(a, dtype=np.uint8)
     b = np.ascontiguousarray(b, dtype=np.uint8)
     D, H, W = a.shape
     if max_trips is None:
         max_trips = W + H + D + 3
     out = ctypes.c_int(-1)
-    rc = _load().ref_forbench_hd(PTX.encode(), a.ctypes.data, b.ctypes.data, W, H, D, max_trips, ctypes.byref(out))
+    rc = _load().ref_forbench_hd(PTX[se].encode(), a.ctypes.data, b.ctypes.data, W, H, D, max_trips,
+                                 ctypes.byref(out))
     if rc == 1:
         raise ValueError("exactly one mask is empty: the reference would loop forever; not run")
     if rc != 0:
