@@ -26,7 +26,7 @@ constexpr int kMaxPairsPerLaunch = 65535;
 // Bounding box and counts of one pair, accumulated by the packing kernel.
 struct PairInfo {
     unsigned long long n_a, n_b, n_ab;
-    int32_t bb[6];  // min x, max x, min y, max y, min z, max z (min = INT_MAX, max = -1 when empty)
+    int32_t bb[6];  // min / max x word, y, z of A u B (min = INT_MAX, max = -1 when empty)
     int32_t pad[2];
 };
 
@@ -57,7 +57,7 @@ struct PairDesc {
 // launch covers the tiles of all pairs.  Packing tiles cover the packed
 // volume (wxf * H * D words), set-up tiles the domain capacity (rows padded
 // to 4 words: roundup(wxf, 4) * H * D).
-constexpr long long kTileWords = 8192;
+constexpr long long kTileWords = 1024;
 __host__ __device__ __forceinline__ long long pack_words(int W, int H, int D) {
     return (long long)((W + 31) / 32) * H * D;
 }

@@ -3,13 +3,14 @@
 // pack_kernel   replaces boolPrepareKernel (hello.cu:539-748) and the bounding
 //               box of getMinMaxes (hello.cu:398-526): uint8 masks -> 32 voxels
 //               per uint32 along x (the prototype packs along z, :598-631),
-//               with |A|, |B|, |A n B| and the bounding box of A u B.  One pass
-//               over the bytes, 128-bit loads.
+//               with |A|, |B|, |A n B| and the bounding box of A u B (x in
+//               whole words).  One pass over the bytes, 128-bit streaming loads.
 // setup_kernel  replaces firstMetaPrepareKernel (hello.cu:763-877): crops the
 //               packed masks to each job's domain, builds the uncovered-target
 //               words, writes the job descriptors and queues every brick of
 //               each job for its first step.
 // map_init_kernel  -1 / 0 initialisation of the optional per-voxel maps.
+#include <algorithm>
 #include <climits>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -19,27 +20,21 @@
 
 namespace hdk {
 
-// Nonzero bytes of a 32-bit word -> 4 bits (byte i -> bit i).
-__device__ __forceinline__ uint32_t nz4(uint32_t w) {
-    uint32_t t = (((w & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | w) & 0x80808080u;
-    // bits 7, 15, 23, 31 -> 28, 29, 30, 31 (products land on distinct bits, no carries)
-    return ((t >> 7) * 0x10204080u) >> 28;
+// Nonzero bytes of a 32-bit word as flags at bits 28..31 (byte i -> bit
+// 28 + i).  The normalised word has bits only at 7, 15, 23, 31; times
+// 2^0 + 2^7 + 2^14 + 2^21 its partial products land on distinct bits (7, 14,
+// 15, 21, 22, 23 below 28, the flags at 28..31), so nothing carries.
+__device__ __forceinline__ uint32_t nz4_top(uint32_t w) {
+    const uint32_t t = (((w & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | w) & 0x80808080u;
+    return t * 0x00204081u;
 }
 
+// Nonzero bytes of 16 bytes -> 16 bits (byte i -> bit i).  The partial
+// products below bit 24 vanish in the two larger shifts and are masked off in
+// the two smaller ones.
 __device__ __forceinline__ uint32_t nz16(uint4 v) {
-    return nz4(v.x) | (nz4(v.y) << 4) | (nz4(v.z) << 8) | (nz4(v.w) << 12);
-}
-
-// 16 mask bits of the 16-byte chunk `ch` of a buffer of n bytes.
-__device__ __forceinline__ uint32_t chunk_bits(const uint8_t* __restrict__ p, long long ch, long long n,
-                                               bool aligned) {
-    const long long s = ch * 16;
-    if (s >= n) return 0u;
-    if (aligned && s + 16 <= n) return nz16(*reinterpret_cast<const uint4*>(p + s));
-    uint32_t bits = 0;
-    const int lim = (int)((n - s) < 16 ? (n - s) : 16);
-    for (int i = 0; i < lim; ++i) bits |= (uint32_t)(p[s + i] != 0) << i;
-    return bits;
+    return (nz4_top(v.x) >> 28) | (nz4_top(v.y) >> 24) | ((nz4_top(v.z) >> 20) & 0xF00u) |
+           ((nz4_top(v.w) >> 16) & 0xF000u);
 }
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
@@ -71,141 +66,242 @@ __device__ __forceinline__ int pair_of_tile(const PairDesc* __restrict__ descs, 
     return lo;
 }
 
-// Bounding-box / count accumulation of one packed word pair.
+// Counts and bounding box of the packed words a thread has seen in one pair.
+// 32-bit counts: a thread packs at most 2^31 / 256 words of a pair.  The
+// box is kept as word columns (x), rows (y) and row indices r = y + H z (z
+// follows at the flush: r -> r / H is monotone).
 struct PackAcc {
-    unsigned long long na = 0, nb = 0, nab = 0;
-    int bb[6] = {INT_MAX, -1, INT_MAX, -1, INT_MAX, -1};
-    __device__ __forceinline__ void add(uint32_t wa, uint32_t wb, long long r, int w, int H) {
+    uint32_t na = 0, nb = 0, nab = 0;
+    int wmin = INT_MAX, wmax = -1, ymin = INT_MAX, ymax = -1, rmin = INT_MAX, rmax = -1;
+    __device__ __forceinline__ void add(uint32_t wa, uint32_t wb, int r, int y, int w) {
         na += __popc(wa);
         nb += __popc(wb);
         nab += __popc(wa & wb);
-        const uint32_t u = wa | wb;
-        if (u) {
-            const int y = (int)(r % H), z = (int)(r / H);
-            bb[0] = min(bb[0], 32 * w + __ffs(u) - 1);
-            bb[1] = max(bb[1], 32 * w + 31 - __clz(u));
-            bb[2] = min(bb[2], y);
-            bb[3] = max(bb[3], y);
-            bb[4] = min(bb[4], z);
-            bb[5] = max(bb[5], z);
+        if (wa | wb) {
+            wmin = min(wmin, w);
+            wmax = max(wmax, w);
+            ymin = min(ymin, y);
+            ymax = max(ymax, y);
+            rmin = min(rmin, r);
+            rmax = max(rmax, r);
         }
     }
 };
 
-// 1D grid, block 256: CTAs stride over the tiles of all pairs (kTileWords
-// packed words per tile).
-//   fast path (rows of whole words, 16-byte aligned masks): word t covers bytes
-//   [32 t, 32 t + 32), read as two 16-byte chunks by two neighbouring lanes;
-//   general path: word by word, three 16-byte chunks around the word's bytes.
-__device__ __forceinline__ void flush_acc(const PairDesc& P, const PackAcc& acc);
-
-__device__ __forceinline__ void pack_tile(const PairDesc& P, long long tile_in_pair);
-
-__global__ void __launch_bounds__(256) pack_kernel(const PairDesc* __restrict__ descs, int npairs,
-                                                   long long ntiles) {
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int pi = pair_of_tile(descs, npairs, tile, false);
-        pack_tile(descs[pi], tile - descs[pi].tile0);
-    }
-}
-
-__device__ __forceinline__ void pack_tile(const PairDesc& P, long long tile_in_pair) {
-    const int W = P.W, H = P.H, wxf = P.wxf;
-    const long long total_all = (long long)wxf * H * P.D;
-    const long long nbytes = (long long)W * H * P.D;
-    const bool aligned = P.aligned != 0;
-    // this tile's words [w_lo, w_hi) of the pair
-    const long long w_lo = tile_in_pair * kTileWords;
-    const long long total = min(total_all, w_lo + kTileWords);
-    const long long tid = threadIdx.x;
-    const long long nthr = blockDim.x;
-    PackAcc acc;
-    if (aligned && (W & 31) == 0) {
-        // Coalesced: per load instruction the warp reads 32 consecutive
-        // 16-byte chunks (512 B); lane l's chunk holds 16 voxels, even lanes
-        // take the odd neighbour's 16 bits and own a word.  A warp handles 4 x
-        // 16 words of each mask per round, all 8 loads issued first.
-        const uint4* a4 = reinterpret_cast<const uint4*>(P.a);
-        const uint4* b4 = reinterpret_cast<const uint4*>(P.b);
-        const int lane = threadIdx.x & 31;
-        const long long warp = tid >> 5, nwarp = nthr >> 5;
-        const long long chunks = 2 * total;  // end of this tile in 16-byte chunks of one mask
-        for (long long c0 = 2 * w_lo + warp * 128; c0 < chunks; c0 += nwarp * 128) {
-            uint4 va[4], vb[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const long long c = c0 + i * 32 + lane;
-                if (c < chunks) {
-                    va[i] = a4[c];
-                    vb[i] = b4[c];
-                } else {
-                    va[i] = vb[i] = make_uint4(0u, 0u, 0u, 0u);
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const uint32_t la = nz16(va[i]), lb = nz16(vb[i]);
-                const uint32_t ha = __shfl_down_sync(0xffffffffu, la, 1);
-                const uint32_t hb = __shfl_down_sync(0xffffffffu, lb, 1);
-                const long long c = c0 + i * 32 + lane;
-                if ((lane & 1) == 0 && c < chunks) {
-                    const long long t = c >> 1;
-                    const uint32_t wa = la | (ha << 16), wb = lb | (hb << 16);
-                    P.pa[t] = wa;
-                    P.pb[t] = wb;
-                    const long long r = t / wxf;
-                    acc.add(wa, wb, r, (int)(t - r * wxf), H);
-                }
-            }
-        }
-    } else {
-        for (long long t = w_lo + tid; t < total; t += nthr) {
-            const long long r = t / wxf;
-            const int w = (int)(t - r * wxf);
-            const long long base = r * W + 32LL * w;
-            const long long ch = base >> 4;
-            const int off = (int)(base & 15);
-            const int nbits = min(32, W - 32 * w);
-            const uint32_t keep = nbits == 32 ? 0xffffffffu : ((1u << nbits) - 1u);
-            uint64_t va = chunk_bits(P.a, ch, nbytes, aligned) |
-                          ((uint64_t)chunk_bits(P.a, ch + 1, nbytes, aligned) << 16);
-            uint64_t vb = chunk_bits(P.b, ch, nbytes, aligned) |
-                          ((uint64_t)chunk_bits(P.b, ch + 1, nbytes, aligned) << 16);
-            if (off) {
-                va |= (uint64_t)chunk_bits(P.a, ch + 2, nbytes, aligned) << 32;
-                vb |= (uint64_t)chunk_bits(P.b, ch + 2, nbytes, aligned) << 32;
-            }
-            const uint32_t wa = (uint32_t)(va >> off) & keep;
-            const uint32_t wb = (uint32_t)(vb >> off) & keep;
-            P.pa[t] = wa;
-            P.pb[t] = wb;
-            acc.add(wa, wb, r, w, H);
-        }
-    }
-    flush_acc(P, acc);
-}
-
+// Block-wide reduction of the accumulators, then one set of atomics per CTA
+// (many CTAs update one PairInfo: per-warp atomics serialise on its lines).
+// Called by all threads of the CTA.
 __device__ __forceinline__ void flush_acc(const PairDesc& P, const PackAcc& acc) {
+    __shared__ unsigned long long s_cnt[3][8];
+    __shared__ int s_bb[6][8];
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     unsigned long long na = warp_sum_u64(acc.na), nb = warp_sum_u64(acc.nb), nab = warp_sum_u64(acc.nab);
-    int bb[6];
-#pragma unroll
-    for (int i = 0; i < 6; i += 2) {
-        bb[i] = warp_min(acc.bb[i]);
-        bb[i + 1] = warp_max(acc.bb[i + 1]);
-    }
+    int bb[6] = {warp_min(acc.wmin), warp_max(acc.wmax), warp_min(acc.ymin),
+                 warp_max(acc.ymax), warp_min(acc.rmin), warp_max(acc.rmax)};
+    __syncthreads();  // earlier readers of the scratch are done
     if ((threadIdx.x & 31) == 0) {
+        s_cnt[0][warp] = na;
+        s_cnt[1][warp] = nb;
+        s_cnt[2][warp] = nab;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) s_bb[i][warp] = bb[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < nwarps; ++w) {
+            na += s_cnt[0][w];
+            nb += s_cnt[1][w];
+            nab += s_cnt[2][w];
+            for (int i = 0; i < 6; i += 2) {
+                bb[i] = min(bb[i], s_bb[i][w]);
+                bb[i + 1] = max(bb[i + 1], s_bb[i + 1][w]);
+            }
+        }
         PairInfo* I = P.info;
         if (na) atomicAdd(&I->n_a, na);
         if (nb) atomicAdd(&I->n_b, nb);
         if (nab) atomicAdd(&I->n_ab, nab);
         if (bb[1] >= 0) {
+            const int H = P.H;
+            atomicMin(&I->bb[0], bb[0]);
+            atomicMax(&I->bb[1], bb[1]);
+            atomicMin(&I->bb[2], bb[2]);
+            atomicMax(&I->bb[3], bb[3]);
+            atomicMin(&I->bb[4], bb[4] / H);
+            atomicMax(&I->bb[5], bb[5] / H);
+        }
+    }
+}
+
+// Nonzero bytes among the 16 at p that lie inside [lo, hi), as 16 bits (a
+// mask's first and last 16-byte chunks may stick out of it).
+__device__ __noinline__ uint32_t chunk_bits_edge(const uint8_t* p, const uint8_t* lo, const uint8_t* hi) {
+    uint32_t bits = 0;
+    for (int i = 0; i < 16; ++i)
+        if (p + i >= lo && p + i < hi && p[i] != 0) bits |= 1u << i;
+    return bits;
+}
+
+constexpr int kPackThreads = 256;
+constexpr int kPackPerThread = 2;  // words per thread and round
+constexpr int kPackRounds = (int)(kTileWords / (kPackThreads * kPackPerThread));
+static_assert(kTileWords % (kPackThreads * kPackPerThread) == 0, "a tile is a whole number of rounds");
+
+// Constants of one pair's packing walk (taken when a CTA's run of tiles
+// enters the pair).
+struct PackWalk {
+    const uint8_t* src[2];
+    const uint8_t* end[2];
+    unsigned wxf, W, H, total;  // words per row, bytes per row, rows per plane, words of the pair
+    unsigned dq, dr;            // kPackThreads words = dq rows + dr words
+    uint32_t tail;              // valid bits of a row's last word
+};
+
+__device__ __forceinline__ PackWalk make_walk(const PairDesc& P) {
+    PackWalk k;
+    const size_t nbytes = (size_t)P.W * P.H * P.D;
+    k.src[0] = P.a;
+    k.src[1] = P.b;
+    k.end[0] = P.a + nbytes;
+    k.end[1] = P.b + nbytes;
+    k.wxf = (unsigned)P.wxf;
+    k.W = (unsigned)P.W;
+    k.H = (unsigned)P.H;
+    k.total = (unsigned)((long long)P.wxf * P.H * P.D);  // < 2^31 words
+    k.dq = kPackThreads / k.wxf;
+    k.dr = kPackThreads - k.dq * k.wxf;
+    const unsigned tb = k.W - 32u * (k.wxf - 1);
+    k.tail = tb >= 32 ? 0xffffffffu : ((1u << tb) - 1u);
+    return k;
+}
+
+// One tile of a pair, any width, alignment or memory kind (device or
+// host-mapped).  In round j thread i packs words w_lo + 512 j + i + 256 k
+// (k = 0, 1) of both masks.  Word (row r, word w) holds the mask bytes
+// [r W + 32 w, + min(32, W - 32 w)), which lie in three 16-byte aligned
+// chunks of memory (two if aligned).  The thread loads the first two; the
+// third is the next lane's first chunk when the next lane holds the next word
+// of the same row, and is loaded with the others otherwise (last lane, end of
+// a row).  A round's loads are all issued before any is used, as streaming
+// loads (each byte is read once).
+// kEdge = false: every word of the tile is in the pair and every chunk it
+// touches lies inside the masks (tiles other than a pair's first and last
+// two, see pack_kernel); kEdge = true: both are checked word by word.
+template <bool kEdge>
+__device__ __forceinline__ void pack_tile(const PairDesc& P, const PackWalk& k, long long tile_in_pair,
+                                          PackAcc& acc) {
+    const int lane = threadIdx.x & 31;
+    const unsigned w_lo = (unsigned)(tile_in_pair * kTileWords);
+    // position of the thread's first word: row r (y + H z) and word w
+    unsigned t = w_lo + threadIdx.x;
+    unsigned r = t / k.wxf, w = t - r * k.wxf;
+    unsigned y = r % k.H;
+#pragma unroll 1
+    for (int j = 0; j < kPackRounds; ++j) {
+        uint4 c[kPackPerThread][2][3];
+        unsigned rr[kPackPerThread], ww[kPackPerThread], yy[kPackPerThread], tt[kPackPerThread];
 #pragma unroll
-            for (int i = 0; i < 6; i += 2) {
-                atomicMin(&I->bb[i], bb[i]);
-                atomicMax(&I->bb[i + 1], bb[i + 1]);
+        for (int i = 0; i < kPackPerThread; ++i) {
+            rr[i] = r;
+            ww[i] = w;
+            yy[i] = y;
+            tt[i] = t;
+            const size_t off = (size_t)r * k.W + 32u * w;
+            const unsigned nbits = w + 1 == k.wxf ? k.W - 32u * w : 32u;
+            const bool next_here = lane < 31 && w + 1 < k.wxf;
+            const bool valid = !kEdge || t < k.total;
+#pragma unroll
+            for (int m = 0; m < 2; ++m) {
+                const uint8_t* x = k.src[m] + off;
+                const uint8_t* q = (const uint8_t*)((uintptr_t)x & ~(uintptr_t)15);
+                const unsigned sh = (unsigned)((uintptr_t)x & 15);
+                const bool third = !next_here && sh + nbits > 32;
+                c[i][m][0] = c[i][m][1] = c[i][m][2] = make_uint4(0u, 0u, 0u, 0u);
+                if (valid && (!kEdge || (q >= k.src[m] && q + 48 <= k.end[m]))) {
+                    c[i][m][0] = __ldcs(reinterpret_cast<const uint4*>(q));
+                    c[i][m][1] = __ldcs(reinterpret_cast<const uint4*>(q) + 1);
+                    if (third) c[i][m][2] = __ldcs(reinterpret_cast<const uint4*>(q) + 2);
+                }
+            }
+            // advance by kPackThreads words
+            t += kPackThreads;
+            w += k.dr;
+            unsigned dy = k.dq;
+            if (w >= k.wxf) {
+                w -= k.wxf;
+                ++dy;
+            }
+            r += dy;
+            y += dy;
+            if (y >= k.H) y %= k.H;
+        }
+#pragma unroll
+        for (int i = 0; i < kPackPerThread; ++i) {
+            const unsigned wi = ww[i], ti = tt[i];
+            const size_t off = (size_t)rr[i] * k.W + 32u * wi;
+            const bool last = wi + 1 == k.wxf;
+            const unsigned nbits = last ? k.W - 32u * wi : 32u;
+            const bool next_here = lane < 31 && !last;
+            const bool valid = !kEdge || ti < k.total;
+            uint32_t out[2];
+#pragma unroll
+            for (int m = 0; m < 2; ++m) {
+                const uint8_t* x = k.src[m] + off;
+                const uint8_t* q = (const uint8_t*)((uintptr_t)x & ~(uintptr_t)15);
+                const unsigned sh = (unsigned)((uintptr_t)x & 15);
+                uint32_t lo, hi;
+                if (kEdge && valid && !(q >= k.src[m] && q + 48 <= k.end[m])) {
+                    lo = chunk_bits_edge(q, k.src[m], k.end[m]) | (chunk_bits_edge(q + 16, k.src[m], k.end[m]) << 16);
+                    hi = chunk_bits_edge(q + 32, k.src[m], k.end[m]);
+                } else {
+                    lo = nz16(c[i][m][0]) | (nz16(c[i][m][1]) << 16);
+                    hi = nz16(c[i][m][2]);
+                }
+                const uint32_t next = __shfl_down_sync(0xffffffffu, lo & 0xffffu, 1);
+                if (next_here) hi = next;
+                out[m] = __funnelshift_r(lo, hi, sh) & (last ? k.tail : 0xffffffffu);
+            }
+            if (valid) {
+                P.pa[ti] = out[0];
+                P.pb[ti] = out[1];
+                acc.add(out[0], out[1], (int)rr[i], (int)yy[i], (int)wi);
             }
         }
     }
+}
+
+// Packing launch: one wave of resident CTAs, each over a contiguous run of
+// tiles (a run crosses few pairs, so the pair lookup and the accumulator
+// flush are rare).  A tile takes the checked path if it is a pair's first
+// tile or reaches within 48 words of the pair's end: every other word then
+// starts at byte >= kTileWords (each word holds >= 1 byte) and ends >= 48
+// bytes before the mask's end, so its three chunks lie inside the mask.
+__global__ void __launch_bounds__(kPackThreads, 2) pack_kernel(const PairDesc* __restrict__ descs, int npairs,
+                                                               long long ntiles) {
+    PackAcc acc;
+    PackWalk walk;
+    int pi = -1;
+    const long long per = (ntiles + gridDim.x - 1) / gridDim.x;
+    const long long t_lo = (long long)blockIdx.x * per, t_hi = min(ntiles, t_lo + per);
+    for (long long tile = t_lo; tile < t_hi; ++tile) {
+        // tiles only increase: walk forward to the owning pair
+        int np = pi < 0 ? pair_of_tile(descs, npairs, tile, false) : pi;
+        while (np + 1 < npairs && descs[np + 1].tile0 <= tile) ++np;
+        if (np != pi) {
+            if (pi >= 0) {
+                flush_acc(descs[pi], acc);
+                acc = PackAcc();
+            }
+            pi = np;
+            walk = make_walk(descs[pi]);
+        }
+        const long long tp = tile - descs[pi].tile0;
+        if (tp >= 1 && (tp + 1) * kTileWords + 48 <= (long long)walk.total)
+            pack_tile<false>(descs[pi], walk, tp, acc);
+        else
+            pack_tile<true>(descs[pi], walk, tp, acc);
+    }
+    if (pi >= 0) flush_acc(descs[pi], acc);
 }
 
 struct Domain {
@@ -218,8 +314,8 @@ __device__ __forceinline__ Domain make_domain(const PairDesc& P, const PairInfo&
         // 6-neighbour element: every shortest path between two voxels of the
         // bounding box of A u B is monotone and stays in it, so cropping to it
         // (x widened to whole words, still inside the volume) is exact.
-        m.wx0 = I.bb[0] >> 5;
-        const int wx1 = I.bb[1] >> 5;
+        m.wx0 = I.bb[0];  // word columns
+        const int wx1 = I.bb[1];
         m.ox = 32 * m.wx0;
         m.wv = min(P.W, 32 * (wx1 + 1)) - m.ox;
         m.oy = I.bb[2];
@@ -251,8 +347,13 @@ __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__
                                                     Job* jobs, JobState* states, unsigned long long* queue0,
                                                     Ctl* ctl, int g0, int bxw, int by, int bz, int stats) {
     (void)stats;
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int pi = pair_of_tile(descs, npairs, tile, true);
+    int pi = -1;
+    const long long per = (ntiles + gridDim.x - 1) / gridDim.x;  // a contiguous run of tiles per CTA
+    const long long t_lo = (long long)blockIdx.x * per, t_hi = min(ntiles, t_lo + per);
+    for (long long tile = t_lo; tile < t_hi; ++tile) {
+        int np = pi < 0 ? pair_of_tile(descs, npairs, tile, true) : pi;
+        while (np + 1 < npairs && descs[np + 1].stile0 <= tile) ++np;  // tiles only increase
+        pi = np;
         setup_tile(descs[pi], tile - descs[pi].stile0, jobs, states, queue0, ctl, g0, bxw, by, bz);
     }
 }
@@ -319,11 +420,14 @@ __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_
     const long long words = min((long long)m.pitch * m.h * m.d, w_hi);
     const bool act0 = rem[0] > 0, act1 = rem[1] > 0;
     for (long long t = w_lo + tid0; t < words; t += nthr) {
-        const long long r = t / m.pitch;
-        const int w = (int)(t - r * m.pitch);
+        // domain word index < 2^31: 32-bit divisions
+        const unsigned tu = (unsigned)t;
+        const unsigned r = tu / (unsigned)m.pitch;
+        const int w = (int)(tu - r * (unsigned)m.pitch);
         uint32_t a = 0, b = 0;
         if (w < m.wx) {
-            const int yl = (int)(r % m.h), zl = (int)(r / m.h);
+            const unsigned zq = r / (unsigned)m.h;
+            const int yl = (int)(r - zq * (unsigned)m.h), zl = (int)zq;
             const long long src = ((long long)(m.oz + zl) * P.H + (m.oy + yl)) * P.wxf + m.wx0 + w;
             a = __ldg(P.pa + src);
             b = __ldg(P.pb + src);
@@ -380,7 +484,22 @@ __global__ void map_init_kernel(const PairDesc* __restrict__ descs, int32_t* map
 namespace hdk {
 
 cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, int grid, cudaStream_t s) {
-    pack_kernel<<<grid, 256, 0, s>>>(d_descs, npairs, ntiles);
+    // one wave of resident CTAs (per device, from the occupancy calculator)
+    static int resident[64] = {0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 64 && resident[dev] == 0) {
+        int per_sm = 0, sms = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pack_kernel, kPackThreads, 0);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        resident[dev] = std::max(1, per_sm) * std::max(1, sms);
+    }
+    if (dev < 64) grid = resident[dev];
+    if (grid > ntiles) grid = (int)ntiles;
+    if (grid < 1) grid = 1;
+    pack_kernel<<<grid, kPackThreads, 0, s>>>(d_descs, npairs, ntiles);
     return cudaGetLastError();
 }
 
