@@ -233,15 +233,17 @@ def bench_ours(args):
     else:
         achieved = None
         alg = None
+    kname = {"solve": "solve_tb_kernel" if phases[-1]["kernel"] == 2 else "solve_kernel",
+             "pack": "pack_kernel", "setup": "setup_kernel"}[dom]
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
-            traffic = json.load(f).get("c2_512x512x256_se6", {}).get(dom)
+            traffic = json.load(f).get("c2_512x512x256_se6", {}).get(kname)
     except Exception:
         traffic = None
     roofline = {
-        "bound": "hbm", "kernel": {"solve": "solve_kernel (persistent frontier dilation)", "pack": "pack_kernel",
-                                   "setup": "setup_kernel"}[dom],
+        "bound": "hbm", "kernel": kname + {"solve": " (persistent frontier dilation)", "pack": " (uint8 -> bits)",
+                                           "setup": " (crop + first queue)"}[dom],
         "achieved": round(achieved, 1) if achieved else None, "peak": peak, "unit": "GB/s",
         "frac": round(achieved / peak, 4) if achieved else None, "peak_source": f"{peak_kind} MEASURED_PEAKS hbm_gbs",
         "traffic": traffic, "algorithmic_bytes": alg,

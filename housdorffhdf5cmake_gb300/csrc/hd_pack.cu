@@ -143,9 +143,8 @@ __device__ __noinline__ uint32_t chunk_bits_edge(const uint8_t* p, const uint8_t
 }
 
 constexpr int kPackThreads = 256;
-constexpr int kPackPerThread = 2;  // words per thread and round
-constexpr int kPackRounds = (int)(kTileWords / (kPackThreads * kPackPerThread));
-static_assert(kTileWords % (kPackThreads * kPackPerThread) == 0, "a tile is a whole number of rounds");
+constexpr int kPackGroups = 4;  // words per thread and tile: a warp packs 32 * kPackGroups consecutive words
+static_assert(kTileWords == (kPackThreads / 32) * 32 * kPackGroups, "one tile = one span per warp");
 
 // Constants of one pair's packing walk (taken when a CTA's run of tiles
 // enters the pair).
@@ -153,7 +152,7 @@ struct PackWalk {
     const uint8_t* src[2];
     const uint8_t* end[2];
     unsigned wxf, W, H, total;  // words per row, bytes per row, rows per plane, words of the pair
-    unsigned dq, dr;            // kPackThreads words = dq rows + dr words
+    unsigned dq, dr;            // 32 words = dq rows + dr words
     uint32_t tail;              // valid bits of a row's last word
 };
 
@@ -168,104 +167,122 @@ __device__ __forceinline__ PackWalk make_walk(const PairDesc& P) {
     k.W = (unsigned)P.W;
     k.H = (unsigned)P.H;
     k.total = (unsigned)((long long)P.wxf * P.H * P.D);  // < 2^31 words
-    k.dq = kPackThreads / k.wxf;
-    k.dr = kPackThreads - k.dq * k.wxf;
+    k.dq = 32u / k.wxf;
+    k.dr = 32u - k.dq * k.wxf;
     const unsigned tb = k.W - 32u * (k.wxf - 1);
     k.tail = tb >= 32 ? 0xffffffffu : ((1u << tb) - 1u);
     return k;
 }
 
 // One tile of a pair, any width, alignment or memory kind (device or
-// host-mapped).  In round j thread i packs words w_lo + 512 j + i + 256 k
-// (k = 0, 1) of both masks.  Word (row r, word w) holds the mask bytes
-// [r W + 32 w, + min(32, W - 32 w)), which lie in three 16-byte aligned
-// chunks of memory (two if aligned).  The thread loads the first two; the
-// third is the next lane's first chunk when the next lane holds the next word
-// of the same row, and is loaded with the others otherwise (last lane, end of
-// a row).  A round's loads are all issued before any is used, as streaming
-// loads (each byte is read once).
+// host-mapped).  Warp v packs words w_lo + 128 v + 32 i + lane (i < 4) of
+// both masks.  Word t (row r, word w) holds the mask bytes [o, o + n) with
+// o = r W + 32 w, n = min(32, W - 32 w); with q = o rounded down to 16 and
+// s = o - q they lie in the 16-byte chunks at q, q + 16 and, if s + n > 32,
+// q + 32.  Rows are contiguous, so word t + 1 starts at o + n, and when
+// s + n > 32 (then 32 < s + n <= 47) its first chunk is the one at q + 32.
+// Each thread therefore loads two chunks per word and takes the third from
+// the thread that holds word t + 1: the next lane, or lane 0's next group
+// for lane 31.  Only lane 31's last group (and a pair's last word) loads a
+// third chunk.  All loads are issued before any is used, as streaming loads.
 // kEdge = false: every word of the tile is in the pair and every chunk it
-// touches lies inside the masks (tiles other than a pair's first and last
-// two, see pack_kernel); kEdge = true: both are checked word by word.
+// touches lies inside the masks (see pack_kernel); kEdge = true: both are
+// checked word by word.
 template <bool kEdge>
 __device__ __forceinline__ void pack_tile(const PairDesc& P, const PackWalk& k, long long tile_in_pair,
                                           PackAcc& acc) {
     const int lane = threadIdx.x & 31;
-    const unsigned w_lo = (unsigned)(tile_in_pair * kTileWords);
-    // position of the thread's first word: row r (y + H z) and word w
-    unsigned t = w_lo + threadIdx.x;
-    unsigned r = t / k.wxf, w = t - r * k.wxf;
+    const unsigned t0 = (unsigned)(tile_in_pair * kTileWords) + (threadIdx.x >> 5) * (32u * kPackGroups) + lane;
+    unsigned r = t0 / k.wxf, w = t0 - r * k.wxf;
     unsigned y = r % k.H;
-#pragma unroll 1
-    for (int j = 0; j < kPackRounds; ++j) {
-        uint4 c[kPackPerThread][2][3];
-        unsigned rr[kPackPerThread], ww[kPackPerThread], yy[kPackPerThread], tt[kPackPerThread];
+    uint4 c[kPackGroups][2][2];
+    uint4 c3[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
+    unsigned rr[kPackGroups], ww[kPackGroups], yy[kPackGroups];
 #pragma unroll
-        for (int i = 0; i < kPackPerThread; ++i) {
-            rr[i] = r;
-            ww[i] = w;
-            yy[i] = y;
-            tt[i] = t;
-            const size_t off = (size_t)r * k.W + 32u * w;
-            const unsigned nbits = w + 1 == k.wxf ? k.W - 32u * w : 32u;
-            const bool next_here = lane < 31 && w + 1 < k.wxf;
-            const bool valid = !kEdge || t < k.total;
+    for (int i = 0; i < kPackGroups; ++i) {
+        rr[i] = r;
+        ww[i] = w;
+        yy[i] = y;
+        const unsigned t = t0 + 32u * i;
+        const size_t off = (size_t)r * k.W + 32u * w;
+        const bool valid = !kEdge || t < k.total;
+        const unsigned nbits = w + 1 == k.wxf ? k.W - 32u * w : 32u;
+        const bool own3 = (i == kPackGroups - 1 && lane == 31) || (kEdge && t + 1 == k.total);
 #pragma unroll
-            for (int m = 0; m < 2; ++m) {
-                const uint8_t* x = k.src[m] + off;
-                const uint8_t* q = (const uint8_t*)((uintptr_t)x & ~(uintptr_t)15);
-                const unsigned sh = (unsigned)((uintptr_t)x & 15);
-                const bool third = !next_here && sh + nbits > 32;
-                c[i][m][0] = c[i][m][1] = c[i][m][2] = make_uint4(0u, 0u, 0u, 0u);
-                if (valid && (!kEdge || (q >= k.src[m] && q + 48 <= k.end[m]))) {
-                    c[i][m][0] = __ldcs(reinterpret_cast<const uint4*>(q));
-                    c[i][m][1] = __ldcs(reinterpret_cast<const uint4*>(q) + 1);
-                    if (third) c[i][m][2] = __ldcs(reinterpret_cast<const uint4*>(q) + 2);
-                }
+        for (int m = 0; m < 2; ++m) {
+            const uint8_t* x = k.src[m] + off;
+            const uint8_t* q = (const uint8_t*)((uintptr_t)x & ~(uintptr_t)15);
+            const unsigned sh = (unsigned)((uintptr_t)x & 15);
+            if (!kEdge || (valid && q >= k.src[m] && q + 48 <= k.end[m])) {
+                c[i][m][0] = __ldcs(reinterpret_cast<const uint4*>(q));
+                c[i][m][1] = __ldcs(reinterpret_cast<const uint4*>(q) + 1);
+                if (own3 && sh + nbits > 32) c3[m] = __ldcs(reinterpret_cast<const uint4*>(q) + 2);
+            } else {
+                c[i][m][0] = c[i][m][1] = make_uint4(0u, 0u, 0u, 0u);
             }
-            // advance by kPackThreads words
-            t += kPackThreads;
-            w += k.dr;
-            unsigned dy = k.dq;
-            if (w >= k.wxf) {
-                w -= k.wxf;
-                ++dy;
-            }
-            r += dy;
-            y += dy;
-            if (y >= k.H) y %= k.H;
         }
+        // next group: 32 words on
+        w += k.dr;
+        unsigned dy = k.dq;
+        if (w >= k.wxf) {
+            w -= k.wxf;
+            ++dy;
+        }
+        r += dy;
+        y += dy;
+        if (y >= k.H) y %= k.H;
+    }
+    // mask bits of each word's first two chunks
+    uint32_t lo[kPackGroups][2];
 #pragma unroll
-        for (int i = 0; i < kPackPerThread; ++i) {
-            const unsigned wi = ww[i], ti = tt[i];
-            const size_t off = (size_t)rr[i] * k.W + 32u * wi;
-            const bool last = wi + 1 == k.wxf;
-            const unsigned nbits = last ? k.W - 32u * wi : 32u;
-            const bool next_here = lane < 31 && !last;
-            const bool valid = !kEdge || ti < k.total;
-            uint32_t out[2];
+    for (int i = 0; i < kPackGroups; ++i) {
+        const size_t off = (size_t)rr[i] * k.W + 32u * ww[i];
+        const unsigned t = t0 + 32u * i;
 #pragma unroll
-            for (int m = 0; m < 2; ++m) {
-                const uint8_t* x = k.src[m] + off;
-                const uint8_t* q = (const uint8_t*)((uintptr_t)x & ~(uintptr_t)15);
-                const unsigned sh = (unsigned)((uintptr_t)x & 15);
-                uint32_t lo, hi;
-                if (kEdge && valid && !(q >= k.src[m] && q + 48 <= k.end[m])) {
-                    lo = chunk_bits_edge(q, k.src[m], k.end[m]) | (chunk_bits_edge(q + 16, k.src[m], k.end[m]) << 16);
-                    hi = chunk_bits_edge(q + 32, k.src[m], k.end[m]);
-                } else {
-                    lo = nz16(c[i][m][0]) | (nz16(c[i][m][1]) << 16);
-                    hi = nz16(c[i][m][2]);
+        for (int m = 0; m < 2; ++m) {
+            if (kEdge) {
+                const uint8_t* q = (const uint8_t*)((uintptr_t)(k.src[m] + off) & ~(uintptr_t)15);
+                if (t < k.total && !(q >= k.src[m] && q + 48 <= k.end[m])) {
+                    lo[i][m] = chunk_bits_edge(q, k.src[m], k.end[m]) |
+                               (chunk_bits_edge(q + 16, k.src[m], k.end[m]) << 16);
+                    continue;
                 }
-                const uint32_t next = __shfl_down_sync(0xffffffffu, lo & 0xffffu, 1);
-                if (next_here) hi = next;
-                out[m] = __funnelshift_r(lo, hi, sh) & (last ? k.tail : 0xffffffffu);
             }
-            if (valid) {
-                P.pa[ti] = out[0];
-                P.pb[ti] = out[1];
-                acc.add(out[0], out[1], (int)rr[i], (int)yy[i], (int)wi);
+            lo[i][m] = nz16(c[i][m][0]) | (nz16(c[i][m][1]) << 16);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < kPackGroups; ++i) {
+        const unsigned t = t0 + 32u * i;
+        const unsigned wi = ww[i];
+        const size_t off = (size_t)rr[i] * k.W + 32u * wi;
+        const bool last = wi + 1 == k.wxf;
+        const unsigned nbits = last ? k.W - 32u * wi : 32u;
+        const bool own3 = (i == kPackGroups - 1 && lane == 31) || (kEdge && t + 1 == k.total);
+        uint32_t out[2];
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+            const unsigned sh = (unsigned)((uintptr_t)(k.src[m] + off) & 15);
+            uint32_t hi = __shfl_down_sync(0xffffffffu, lo[i][m] & 0xffffu, 1);
+            if (i + 1 < kPackGroups) {
+                const uint32_t wrap = __shfl_sync(0xffffffffu, lo[i + 1 < kPackGroups ? i + 1 : i][m] & 0xffffu, 0);
+                if (lane == 31) hi = wrap;
             }
+            if (own3 && sh + nbits > 32) {  // rare: the warp's last word, the pair's last word
+                if (kEdge) {
+                    const uint8_t* q = (const uint8_t*)((uintptr_t)(k.src[m] + off) & ~(uintptr_t)15);
+                    hi = (q >= k.src[m] && q + 48 <= k.end[m]) ? nz16(c3[m])  // loaded above
+                                                                : chunk_bits_edge(q + 32, k.src[m], k.end[m]);
+                } else {
+                    hi = nz16(c3[m]);
+                }
+            }
+            out[m] = __funnelshift_r(lo[i][m], hi, sh) & (last ? k.tail : 0xffffffffu);
+        }
+        if (!kEdge || t < k.total) {
+            P.pa[t] = out[0];
+            P.pb[t] = out[1];
+            acc.add(out[0], out[1], (int)rr[i], (int)yy[i], (int)wi);
         }
     }
 }
@@ -348,9 +365,9 @@ __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__
                                                     Ctl* ctl, int g0, int bxw, int by, int bz, int stats) {
     (void)stats;
     int pi = -1;
-    const long long per = (ntiles + gridDim.x - 1) / gridDim.x;  // a contiguous run of tiles per CTA
-    const long long t_lo = (long long)blockIdx.x * per, t_hi = min(ntiles, t_lo + per);
-    for (long long tile = t_lo; tile < t_hi; ++tile) {
+    // CTAs stride over the tiles: a pair's domain fills only the first of
+    // its tiles, so contiguous runs would leave some CTAs without work
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         int np = pi < 0 ? pair_of_tile(descs, npairs, tile, true) : pi;
         while (np + 1 < npairs && descs[np + 1].stile0 <= tile) ++np;  // tiles only increase
         pi = np;
