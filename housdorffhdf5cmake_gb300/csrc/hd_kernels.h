@@ -14,6 +14,8 @@ cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, i
 cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int grid, Job* jobs,
                          JobState* states, unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
                          int stats, cudaStream_t s);
+// Start values of descs[i].info (counts 0, empty bounding box), i < npairs.
+cudaError_t launch_info_init(const PairDesc* d_descs, int npairs, cudaStream_t s);
 cudaError_t launch_zero_i32(int32_t* p, long long n, cudaStream_t s);
 cudaError_t launch_map_init(const PairDesc* d_descs, int32_t* map_a, int32_t* map_b, long long n,
                             cudaStream_t s);

@@ -475,6 +475,17 @@ __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_
     }
 }
 
+// Start values of each pair's counts and bounding box (one thread per pair).
+__global__ void info_init_kernel(const PairDesc* __restrict__ descs, int npairs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npairs) return;
+    PairInfo* I = descs[i].info;
+    I->n_a = I->n_b = I->n_ab = 0ull;
+    I->bb[0] = I->bb[2] = I->bb[4] = INT_MAX;
+    I->bb[1] = I->bb[3] = I->bb[5] = -1;
+    I->pad[0] = I->pad[1] = 0;
+}
+
 // Instrumented runs: zero the per-tile stamps and per-step tile counters.
 __global__ void zero_i32_kernel(int32_t* p, long long n) {
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
@@ -524,6 +535,12 @@ cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, 
                          JobState* states, unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
                          int stats, cudaStream_t s) {
     setup_kernel<<<grid, 256, 0, s>>>(d_descs, npairs, ntiles, jobs, states, queue0, ctl, g0, bxw, by, bz, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_info_init(const PairDesc* d_descs, int npairs, cudaStream_t s) {
+    if (npairs <= 0) return cudaSuccess;
+    info_init_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(d_descs, npairs);
     return cudaGetLastError();
 }
 

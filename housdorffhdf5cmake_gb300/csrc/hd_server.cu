@@ -128,7 +128,8 @@ struct hd_server {
     unsigned long long* d_queue[3] = {nullptr, nullptr, nullptr};
     int32_t* d_stamps = nullptr;
     PairDesc* d_descs = nullptr;      // per-tick admission descriptors
-    int max_admit = 64;
+    int max_admit = 256;
+    cudaMemPool_t pool = nullptr;     // the pairs' buffers: a private pool that keeps what it has reserved
     void* h_pinned = nullptr;         // descriptors out, states in
     size_t h_pinned_bytes = 0;
     int g_next = 1;
@@ -173,6 +174,8 @@ void complete(hd_server* s, Request* r, hd_status st) {
 
 // One scheduler tick.  Called with the server lock NOT held.
 void tick(hd_server* s) {
+    using clk = std::chrono::steady_clock;
+    const auto t_begin = clk::now();
     std::vector<Request*> admit;
     {
         std::lock_guard<std::mutex> lk(s->mu);
@@ -225,8 +228,8 @@ void tick(hd_server* s) {
         Request* r = admit[i];
         void* res = nullptr;
         void* tr = nullptr;
-        e = cudaMallocAsync(&res, r->resident_bytes, st);
-        if (e == cudaSuccess) e = cudaMallocAsync(&tr, r->transient_bytes, st);
+        e = cudaMallocFromPoolAsync(&res, r->resident_bytes, s->pool, st);
+        if (e == cudaSuccess) e = cudaMallocFromPoolAsync(&tr, r->transient_bytes, s->pool, st);
         if (e != cudaSuccess) {
             cudaGetLastError();
             if (res) cudaFreeAsync(res, st);
@@ -282,18 +285,11 @@ void tick(hd_server* s) {
         admitted.push_back(r);
     }
     if (!admitted.empty()) {
-        // info initial values, then descriptors
-        std::vector<PairInfo> init(admitted.size());
-        for (auto& I : init) {
-            std::memset(&I, 0, sizeof I);
-            I.bb[0] = I.bb[2] = I.bb[4] = 0x7fffffff;
-            I.bb[1] = I.bb[3] = I.bb[5] = -1;
-        }
+        // descriptors, then the pairs' count / bounding-box start values
         char* hp = (char*)s->h_pinned + align_up(sizeof(Ctl)) + align_up(sizeof(JobState) * 2 * s->slots.size());
         std::memcpy(hp, descs.data(), sizeof(PairDesc) * descs.size());
         e = cudaMemcpyAsync(s->d_descs, hp, sizeof(PairDesc) * descs.size(), cudaMemcpyHostToDevice, st);
-        for (size_t i = 0; i < admitted.size() && e == cudaSuccess; ++i)
-            e = cudaMemcpyAsync(descs[i].info, &init[i], sizeof(PairInfo), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = hdk::launch_info_init(s->d_descs, (int)descs.size(), st);
         const int cap_ctas = std::max(s->ctx->sm_count * 8, 1);
         if (e == cudaSuccess)
             e = hdk::launch_pack(s->d_descs, (int)admitted.size(), ptiles, (int)std::min<long long>(cap_ctas, ptiles), st);
@@ -302,9 +298,10 @@ void tick(hd_server* s) {
                                   s->d_jobs, s->d_states,
                                   s->d_queue[s->g_next % 3], s->d_ctl, s->g_next, s->shape.bxw, s->shape.by,
                                   s->shape.bz, 0, st);
-        // pageable sources of cudaMemcpyAsync and the info initialisers must
-        // outlive the copies: wait for the admission work before going on
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        // no wait here: the host masks' copies read the requests' own
+        // buffers (alive until completion), the descriptors' staging area is
+        // rewritten only after the end-of-tick synchronisation, and the
+        // transient buffers below are freed in stream order
         if (e != cudaSuccess) {
             cuda_err(s, e, "admission");
         }
@@ -315,6 +312,7 @@ void tick(hd_server* s) {
         std::lock_guard<std::mutex> lk(s->mu);
         for (auto* r : admitted) s->stats.bytes_in_use -= r->transient_bytes;
     }
+    const auto t_admitted = clk::now();
     // ---- one tick of the persistent dilation loop ---------------------------
     int resident = 0;
     for (auto* r : s->slots) resident += r != nullptr;
@@ -350,12 +348,15 @@ void tick(hd_server* s) {
         hard_err = hctl->err;
     }
     if (s->debug) {
+        const auto t_read = clk::now();
         std::fprintf(stderr,
                      "[hd_server] tick %llu admitted %zu resident %d g_next %d err %d(%s) jobs_active %d q %u/%u/%u "
-                     "iters %d\n",
+                     "iters %d admission %.3f ms solve+readback %.3f ms\n",
                      (unsigned long long)s->stats.ticks, admitted.size(), resident, s->g_next, hctl->err,
                      e == cudaSuccess ? "ok" : cudaGetErrorString(e), hctl->jobs_active, hctl->qcount[0],
-                     hctl->qcount[1], hctl->qcount[2], hctl->iters_run);
+                     hctl->qcount[1], hctl->qcount[2], hctl->iters_run,
+                     std::chrono::duration<double, std::milli>(t_admitted - t_begin).count(),
+                     std::chrono::duration<double, std::milli>(t_read - t_admitted).count());
         for (size_t sl = 0; sl < s->slots.size() && sl < 4; ++sl)
             if (s->slots[sl])
                 std::fprintf(stderr, "[hd_server]   slot %zu: active %d/%d remaining %llu/%llu hd %d/%d status %d/%d\n", sl,
@@ -525,6 +526,19 @@ hd_status hd_server_create(hd_context* ctx, const hd_server_options* opt, hd_ser
         s->brick_cap = std::min<unsigned long long>(s->opt.hbm_budget_bytes / (3 * brick_bytes) + 4096, 1ULL << 26);
         s->bricks = RangeAlloc(s->brick_cap);
         cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) {
+            // buffers come and go every tick: a pool that returns memory to
+            // the device at each synchronisation would map and unmap it
+            // every tick, so this one keeps up to the budget reserved
+            cudaMemPoolProps props{};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.handleTypes = cudaMemHandleTypeNone;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = ctx->device;
+            e = cudaMemPoolCreate(&s->pool, &props);
+            uint64_t keep = s->opt.hbm_budget_bytes;
+            if (e == cudaSuccess) e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
         if (e == cudaSuccess) e = cudaMalloc(&s->d_jobs, sizeof(Job) * 2 * slots);
         if (e == cudaSuccess) e = cudaMalloc(&s->d_states, sizeof(JobState) * 2 * slots);
         if (e == cudaSuccess) e = cudaMalloc(&s->d_ctl, sizeof(Ctl));
@@ -640,9 +654,10 @@ hd_status hd_server_destroy(hd_server* s) {
     if (s->worker.joinable()) s->worker.join();
     {
         DeviceGuard g(s->ctx->device);
-        if (s->stream) cudaStreamSynchronize(s->stream);
         for (auto* r : s->slots)
-            if (r && r->resident) cudaFree(r->resident);
+            if (r && r->resident) cudaFreeAsync(r->resident, s->stream);
+        if (s->stream) cudaStreamSynchronize(s->stream);
+        if (s->pool) cudaMemPoolDestroy(s->pool);
         cudaFree(s->d_jobs);
         cudaFree(s->d_states);
         cudaFree(s->d_ctl);
