@@ -532,6 +532,33 @@ def bench_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_case(args):
+    """One workload, run a few times with nothing else around it, for
+    profiler captures (no JSON line): c2 = the 512x512x256 pair (seed 1234),
+    c3 = the 512^3 far-blobs pair, batch = the first --pairs pairs of the
+    256-pair ragged batch in one launch."""
+    import torch
+
+    import housdorffhdf5cmake_gb300 as hd
+    from housdorffhdf5cmake_gb300 import synth
+    ctx = hd.Context(0, record_timings=True)
+    if args.case == "batch":
+        specs = synth.batch_ragged_specs(77, n=256)[: args.pairs]
+        pairs = [synth.pair_from_spec(s, "cuda") for s in specs]
+        run = lambda: ctx.batch(pairs, "se6")
+    else:
+        if args.case == "c2":
+            a, b = synth.pair_shifted_union(1234, (D_, H_, W_), "cuda")
+        else:
+            a, b = synth.pair_far_blobs(5, (512, 512, 512), "cuda")
+        run = lambda: ctx.compute(a, b, "se6")
+    for _ in range(args.repeat):
+        run()
+    torch.cuda.synchronize()
+    print(args.case, json.dumps(ctx.last_timings()), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -540,7 +567,14 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and worst-case sub-results")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--case", choices=["c2", "c3", "batch"], default=None,
+                    help="run one workload --repeat times for a profiler capture (no JSON line)")
+    ap.add_argument("--repeat", type=int, default=3)
+    ap.add_argument("--pairs", type=int, default=64)
     args = ap.parse_args()
+    if args.case:
+        run_case(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
