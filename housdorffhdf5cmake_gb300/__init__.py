@@ -93,6 +93,14 @@ def _check(code: int, ctx_handle, allow_empty=True):
     raise HDError(code, msg)
 
 
+def _ready(*bufs):
+    """Entry points without a stream argument run on the context's own
+    stream: finish the work that produced CUDA masks on torch's stream."""
+    if any(b.on_device for b in bufs):
+        import torch
+        torch.cuda.current_stream().synchronize()
+
+
 def _current_stream_ptr():
     import torch
     return torch.cuda.current_stream().cuda_stream
@@ -208,6 +216,7 @@ class Context:
             descs[i].metric = metric_code(metric)
             descs[i].on_device = 1 if A.on_device else 0
         res = (N.HdResult * n)()
+        _ready(*[x for ab in bufs for x in ab])
         code = N.load().hd_batch_compute(self._h, descs, n, res)
         _check(code, self._h)
         return [res[i].as_dict() for i in range(n)]
@@ -226,6 +235,7 @@ class Context:
         bricks = ctypes.c_uint64(0)
         r = N.HdResult()
         u64p = ctypes.POINTER(ctypes.c_uint64)
+        _ready(A, B)
         code = N.load().hd_profile_u8_device(self._h, A.ptr, B.ptr, A.W, A.H, A.D, metric_code(metric),
                                              ctypes.byref(r), tab.ctypes.data_as(u64p),
                                              tba.ctypes.data_as(u64p), n, ctypes.byref(bricks))
@@ -242,6 +252,7 @@ class Context:
         ma = torch.empty(A.obj.shape, dtype=torch.int32, device=A.obj.device)
         mb = torch.empty(A.obj.shape, dtype=torch.int32, device=A.obj.device)
         r = N.HdResult()
+        _ready(A, B)  # also orders the maps' allocation before the library writes them
         code = N.load().hd_distance_map_device(self._h, A.ptr, B.ptr, A.W, A.H, A.D, metric_code(metric),
                                                ma.data_ptr(), mb.data_ptr(), ctypes.byref(r))
         _check(code, self._h)
@@ -259,6 +270,7 @@ class Context:
             descs[i].metric = metric_code(metric)
             descs[i].on_device = 1 if A.on_device else 0
         rep = ctypes.create_string_buffer(8192)
+        _ready(*[x for ab in bufs for x in ab])
         code = N.load().hd_autotune(self._h, descs, n, int(repeats), rep, len(rep))
         _check(code, self._h, allow_empty=False)
         return rep.value.decode()

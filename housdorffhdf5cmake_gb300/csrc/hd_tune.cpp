@@ -168,8 +168,12 @@ extern "C" hd_status hd_autotune(hd_context* ctx, const hd_pair_desc* pairs, int
             } else {
                 for (int i = 0; i < n; ++i)
                     if (res[i].hd != ref[i].hd || res[i].sum_ab != ref[i].sum_ab || res[i].sum_ba != ref[i].sum_ba)
-                        return set_error(ctx, HD_ERR_CUDA, "autotune: kernel %d shape %dx%dx%d gave a different result",
-                                         c.kernel, c.bxw, c.by, c.bz);
+                        return set_error(ctx, HD_ERR_CUDA,
+                                         "autotune: kernel %d shape %dx%dx%d steps %d gave a different result on pair %d "
+                                         "(hd %d sums %llu/%llu, first shape: hd %d sums %llu/%llu)",
+                                         c.kernel, c.bxw, c.by, c.bz, c.steps, i, res[i].hd,
+                                         (unsigned long long)res[i].sum_ab, (unsigned long long)res[i].sum_ba, ref[i].hd,
+                                         (unsigned long long)ref[i].sum_ab, (unsigned long long)ref[i].sum_ba);
             }
             std::vector<double> t;
             for (int r = 0; r < repeats; ++r) {

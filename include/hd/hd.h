@@ -157,7 +157,10 @@ typedef struct hd_pair_desc {
 /* Solves n pairs of independent shapes with one packing launch, one set-up
  * launch and ONE persistent dilation launch over a shared (pair, brick) work
  * queue.  Per-pair results are bit-identical to hd_compute_u8.  out[i].status
- * is the status of pair i; the return value is the first hard error. */
+ * is the status of pair i; the return value is the first hard error.
+ * This call, hd_profile_u8_device, hd_distance_map_device and hd_autotune run
+ * on the context's own (non-blocking) stream: device masks must be complete
+ * before the call (synchronise the stream that wrote them). */
 hd_status hd_batch_compute(hd_context* ctx, const hd_pair_desc* pairs, int32_t n, hd_result* out);
 
 /* Instrumented run (not for timing): also returns, per direction, the number

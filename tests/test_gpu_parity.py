@@ -282,3 +282,19 @@ def test_reference_class_mirror(hd, oracle):
     assert d == o["hd"] and avg == o["avg_hd"]
     empty = hd.Volume(64, 64, 64)
     assert h.computeDistance(v1, empty) == -1
+
+
+def test_context_stream_calls_wait_for_torch_stream(hd, ctx):
+    """batch / autotune run on the context's own stream: masks produced on
+    torch's stream just before the call must be complete when they are read."""
+    from housdorffhdf5cmake_gb300 import synth
+    keys = ("hd", "hd_ab", "hd_ba", "sum_ab", "sum_ba", "n_a", "n_b", "status")
+    pairs = [synth.pair_shifted_union(900 + i, (192, 256, 256), "cuda", rmin=8, rmax=60, max_shift=9)
+             for i in range(3)]
+    got = ctx.batch(pairs, "se6")  # no synchronisation between generation and the call
+    want = [ctx.compute(a, b, "se6") for a, b in pairs]
+    for g, w in zip(got, want):
+        assert all(g[k] == w[k] for k in keys), (g, w)
+    more = [synth.pair_shifted_union(950, (192, 256, 256), "cuda", rmin=8, rmax=60, max_shift=9)]
+    with hd.Context(0) as c:
+        c.autotune(more, "se6", repeats=1)  # raises if shapes disagree (a half-written mask would)
