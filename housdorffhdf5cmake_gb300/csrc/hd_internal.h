@@ -42,12 +42,12 @@ struct Shape {  // default: the autotuner's choice on the 512x512x256, 512^3 and
     int smem = 0;       // dynamic shared memory per CTA
     void finish() {
         if (kernel == 2) {
-            // 4 warps per CTA, each staging (bz + 2 steps) planes x 32 rows x 32 B
-            // of state and bz x 32 rows x 16 B of uncovered-target words
+            // kTbWarps warps per CTA, each with a ring of streamed planes and
+            // the brick's uncovered-target rows in shared memory
             bxw = 4;
             by = 32 - 2 * steps;
-            threads = 128;
-            smem = 4 * ((bz + 2 * steps) * 32 * 32 + bz * 32 * 16);
+            threads = hdk::kTbWarps * 32;
+            smem = hdk::kTbWarps * hdk::tb_warp_bytes(steps, bz);
         } else {
             by = 32 / bxw;
             steps = 1;

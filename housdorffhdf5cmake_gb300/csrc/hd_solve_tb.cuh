@@ -10,9 +10,17 @@
 //             and below the interior), streamed plane by plane along z from
 //             z0 - T to z0 + BZ + T - 1
 //   levels    level 0 is the loaded state; level s is the state after s
-//             steps, computed one plane behind level s - 1 from a window of
-//             three of its planes; rows come from the neighbouring lanes by
-//             shuffle, x carries from the neighbouring words of the row
+//             steps, computed one plane behind level s - 1 from three of its
+//             planes; rows come from the neighbouring lanes by shuffle, x
+//             carries from the neighbouring words of the row
+//   staging   planes arrive by cp.async (zero fill outside the domain).  With
+//             T = 4 every plane is copied when the item is issued, before
+//             the previous item's epilogue (shortest item latency; 2 CTAs
+//             per SM).  With T < 4 they go through a ring of shared-memory
+//             slots three planes ahead of the one being computed, and each
+//             level keeps only the pending plane's partial result and the
+//             last plane's z terms in registers, which makes room for a
+//             third CTA per SM
 //
 // Level s is exact on rows [s, 32 - s) and planes [s, BZ + 2T - s) of the
 // streamed block (errors from the unknown outside creep in one voxel per
@@ -32,29 +40,59 @@
 
 namespace hdk {
 
-// Shared memory per warp: the streamed rows (32 B each: 4 interior words,
-// the two halo words, 2 pad words) for NP planes, and the interior
-// uncovered-target words (16 B per row) for BZ planes.
-template <int T, int BZ>
-struct TbSmem {
-    static constexpr int NP = BZ + 2 * T;
-    static constexpr int kRowBytes = 32;
-    static constexpr int kURowBytes = 16;
-    static constexpr int kInBytes = NP * 32 * kRowBytes;
-    static constexpr int kWarpBytes = kInBytes + BZ * 32 * kURowBytes;
-};
-
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
 }
 __device__ __forceinline__ void cp_async4(uint32_t dst, const void* src, uint32_t src_bytes) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() {
-    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+// Waits until at most n groups are pending (n known at compile time after
+// unrolling; counts above N wait for N, which is stricter).
+template <int N>
+__device__ __forceinline__ void cp_async_wait_upto(int n) {
+    if constexpr (N == 0) {
+        cp_async_wait<0>();
+    } else {
+        if (n >= N) cp_async_wait<N>();
+        else cp_async_wait_upto<N - 1>(n);
+    }
 }
 
-// One queue item of the blocked kernel, decoded and with its copies issued.
+// All-planes staging, shared memory per warp: the streamed rows (32 B each:
+// 4 interior words, the two halo words, 2 pad words) for NP planes, and the
+// interior uncovered-target words (16 B per row) for BZ planes.
+template <int T, int BZ>
+struct TbSmemAll {
+    static constexpr int NP = BZ + 2 * T;
+    static constexpr int kRowBytes = 32;
+    static constexpr int kURowBytes = 16;
+    static constexpr int kInBytes = NP * 32 * kRowBytes;
+    static constexpr int kWarpBytes = kInBytes + BZ * 32 * kURowBytes;
+    static_assert(kWarpBytes == tb_warp_bytes(T, BZ), "shared layout");
+};
+
+// Ring staging, shared memory of one warp: ring slots of streamed planes (interior words
+// as 16-byte rows, then the two halo words of each row), then the brick's
+// uncovered-target rows.
+template <int T, int BZ>
+struct TbSmemRing {
+    static constexpr int NP = BZ + 2 * T;  // planes streamed per brick
+    static constexpr int R = tb_ring_slots(T, BZ);
+    static constexpr int PF = tb_prefetch(T, BZ);  // planes in flight ahead of the one computed
+    static constexpr int kInBytes = R * 32 * 16;
+    static constexpr int kHaloBytes = R * 32 * 8;
+    static constexpr int kUOff = kInBytes + kHaloBytes;
+    static constexpr int kWarpBytes = kUOff + BZ * 32 * 16;
+    static_assert(kWarpBytes == tb_warp_bytes(T, BZ), "shared layout");
+    static_assert(R >= T + 1 + PF || R == NP, "a plane must stay until its final step");
+};
+
+// One queue item of the blocked kernel, decoded.
 struct TbItem {
     const Job* Jp;
     JobState* st;
@@ -66,16 +104,64 @@ struct TbItem {
     bool live;
 };
 
-// Decodes a queue entry, checks that its job still needs work, and issues
-// every copy of the brick into the warp's shared memory (rows, planes and
-// halo words outside the domain are zero-filled).  No wait.
+// Where this lane's row of a streamed plane comes from.
+struct TbRow {
+    const uint32_t* src;  // level-0 state of the job (this item's ping-pong buffer)
+    int plane, rowoff, z0, Dd;
+    bool rowv, hl_ok, hr_ok;
+};
+
 template <int T, int BZ>
-__device__ __forceinline__ void tb_issue(const SolveParams& p, unsigned long long e, int g, unsigned char* wsm,
+__device__ __forceinline__ TbRow tb_row(const TbItem& it) {
+    constexpr int IW = 4;
+    constexpr int BYI = 32 - 2 * T;
+    const int lane = threadIdx.x & 31;
+    const Job* Jp = it.Jp;
+    TbRow w;
+    const int Wx = Jp->wx, Hd = Jp->h;
+    const int wx0 = it.bx * IW;
+    const int y = it.by * BYI - T + lane;
+    w.rowv = y >= 0 && y < Hd;
+    w.src = Jp->buf[it.iter & 1];
+    w.plane = Jp->pitch * Hd;
+    w.rowoff = (w.rowv ? y : 0) * Jp->pitch + wx0;
+    w.z0 = it.bz * BZ;
+    w.Dd = Jp->d;
+    w.hl_ok = w.rowv && wx0 > 0;
+    w.hr_ok = w.rowv && wx0 + IW < Wx;
+    return w;
+}
+
+// Copies streamed plane r of the brick into its ring slot (one group).
+template <int T, int BZ>
+__device__ __forceinline__ void tb_copy_plane(const TbRow& w, int r, unsigned char* wsm) {
+    using SM = TbSmemRing<T, BZ>;
+    constexpr int IW = 4;
+    const int lane = threadIdx.x & 31;
+    const int z = w.z0 - T + r;
+    const bool ok = w.rowv && z >= 0 && z < w.Dd;
+    const uint32_t* gp = w.src + (ok ? z * w.plane + w.rowoff : 0);
+    const int slot = r % SM::R;
+    const uint32_t base = (uint32_t)__cvta_generic_to_shared(wsm);
+    const uint32_t s_in = base + (uint32_t)((slot * 32 + lane) * 16);
+    const uint32_t s_h = base + SM::kInBytes + (uint32_t)((slot * 32 + lane) * 8);
+    cp_async16(s_in, gp, ok ? 16u : 0u);
+    cp_async4(s_h, (ok && w.hl_ok) ? gp - 1 : gp, (ok && w.hl_ok) ? 4u : 0u);
+    cp_async4(s_h + 4, (ok && w.hr_ok) ? gp + IW : gp, (ok && w.hr_ok) ? 4u : 0u);
+    cp_async_commit();
+}
+
+// All-planes staging: decodes a queue entry, checks that its job still needs
+// work, and issues every copy of the brick into the warp's shared memory
+// (rows, planes and halo words outside the domain are zero-filled) as one
+// group.  No wait.
+template <int T, int BZ>
+__device__ __forceinline__ void tb_issue_all(const SolveParams& p, unsigned long long e, int g, unsigned char* wsm,
                                          TbItem& it) {
     constexpr int IW = 4;
     constexpr int BYI = 32 - 2 * T;
     constexpr int NP = BZ + 2 * T;
-    using SM = TbSmem<T, BZ>;
+    using SM = TbSmemAll<T, BZ>;
     const int lane = threadIdx.x & 31;
     it.jid = (int)((e >> 32) & 0xffffffu);
     it.lb = (unsigned)e;
@@ -135,6 +221,52 @@ __device__ __forceinline__ void tb_issue(const SolveParams& p, unsigned long lon
     asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
+// Ring staging: decodes a queue entry, checks that its job still needs work, and issues
+// the copies of the brick's uncovered-target rows (one group) and of its
+// first planes (one group each).  No wait.
+template <int T, int BZ>
+__device__ __forceinline__ void tb_issue_ring(const SolveParams& p, unsigned long long e, int g, unsigned char* wsm,
+                                         TbItem& it) {
+    using SM = TbSmemRing<T, BZ>;
+    const int lane = threadIdx.x & 31;
+    it.jid = (int)((e >> 32) & 0xffffffu);
+    it.lb = (unsigned)e;
+    it.epoch = (unsigned)(e >> 56);
+    it.st = p.states + it.jid;
+    it.Jp = p.jobs + it.jid;
+    it.live = false;
+    if (ld_relaxed_s32(&it.st->active) == 0) return;     // nothing left to cover
+    const Job* Jp = it.Jp;
+    if ((Jp->epoch & 0xffu) != it.epoch) return;         // left over from the slot's previous pair
+    it.iter = g - Jp->k0;
+    it.kb = it.iter * T;
+    if (it.kb + 1 > Jp->kmax) {
+        if (lane == 0) {
+            it.st->status = kErrIterLimit;
+            atomicCAS(&p.ctl->err, 0, kErrIterLimit);
+        }
+        return;
+    }
+    const int nbx = Jp->nbx, nby = Jp->nby;
+    it.bx = (int)(it.lb % (unsigned)nbx);
+    const unsigned tq = it.lb / (unsigned)nbx;
+    it.by = (int)(tq % (unsigned)nby);
+    it.bz = (int)(tq / (unsigned)nby);
+    it.live = true;
+    const TbRow w = tb_row<T, BZ>(it);
+    const bool inter = w.rowv && lane >= T && lane < 32 - T;
+    const uint32_t s_u = (uint32_t)__cvta_generic_to_shared(wsm) + SM::kUOff;
+#pragma unroll
+    for (int i = 0; i < BZ; ++i) {
+        const int z = w.z0 + i;
+        const bool ok = inter && z < w.Dd;
+        cp_async16(s_u + (uint32_t)((i * 32 + lane) * 16), Jp->U + (ok ? z * w.plane + w.rowoff : 0), ok ? 16u : 0u);
+    }
+    cp_async_commit();
+#pragma unroll
+    for (int r = 0; r < SM::PF && r < SM::NP; ++r) tb_copy_plane<T, BZ>(w, r, wsm);
+}
+
 // What the epilogue of an item needs from its compute phase.
 constexpr int kTbMaxSteps = 4;
 struct TbOut {
@@ -142,16 +274,17 @@ struct TbOut {
     bool any, fxl, fxh, fyl, fyh, fzl, fzh;
 };
 
-// Waits for the item's copies, runs its T steps and writes its state and
-// uncovered-target words back.
+// All-planes staging: waits for the item's copies, runs its T steps (per
+// level a window of M for two planes and Z for three) and writes its state
+// and uncovered-target words back.
 template <int T, int BZ, bool SE18>
-__device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& it, unsigned char* wsm, TbOut& res) {
+__device__ __forceinline__ void tb_compute_all(const SolveParams& p, const TbItem& it, unsigned char* wsm, TbOut& res) {
     static_assert(T >= 1 && T <= kTbMaxSteps, "steps per barrier out of range");
     constexpr int IW = 4;
     constexpr int NW = IW + 2;
     constexpr int BYI = 32 - 2 * T;
     constexpr int NP = BZ + 2 * T;
-    using SM = TbSmem<T, BZ>;
+    using SM = TbSmemAll<T, BZ>;
     const int lane = threadIdx.x & 31;
     const Job* Jp = it.Jp;
     const int Wx = Jp->wx, Hd = Jp->h, Dd = Jp->d;
@@ -313,6 +446,192 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
     res.fzh = __any_sync(kFull, d_zh != 0);
 }
 
+// Ring staging: runs the item's T steps plane by plane, copying planes into
+// the ring PF ahead (per level the pending plane's partial result and the
+// last plane's Z), and writes its state and uncovered-target words back.
+template <int T, int BZ, bool SE18>
+__device__ __forceinline__ void tb_compute_ring(const SolveParams& p, const TbItem& it, unsigned char* wsm, TbOut& res) {
+    static_assert(T >= 1 && T <= kTbMaxSteps, "steps per barrier out of range");
+    constexpr int IW = 4;
+    constexpr int NW = IW + 2;
+    constexpr int BYI = 32 - 2 * T;
+    using SM = TbSmemRing<T, BZ>;
+    constexpr int NP = SM::NP;
+    const int lane = threadIdx.x & 31;
+    const Job* Jp = it.Jp;
+    const TbRow w = tb_row<T, BZ>(it);
+    const int Wx = Jp->wx;
+    const int wx0 = it.bx * IW;
+    const bool inter = w.rowv && lane >= T && lane < 32 - T;
+    uint32_t* __restrict__ dst = Jp->buf[(it.iter + 1) & 1];
+    uint32_t* __restrict__ U = Jp->U;
+    uint32_t wm[NW];  // valid bits of each word of this lane's row
+#pragma unroll
+    for (int j = 0; j < NW; ++j) {
+        const int x = wx0 - 1 + j;
+        wm[j] = (w.rowv && x >= 0 && x < Wx) ? (x == Wx - 1 ? Jp->tailmask : kFull) : 0u;
+    }
+
+    auto plane_ok = [&](int r) {  // streamed plane index r -> inside the domain
+        const int z = w.z0 - T + r;
+        return z >= 0 && z < w.Dd;
+    };
+    auto in_row = [&](int r) -> uint4 {
+        return *reinterpret_cast<const uint4*>(wsm + ((r % SM::R) * 32 + lane) * 16);
+    };
+    auto halo_row = [&](int r) -> uint2 {
+        return *reinterpret_cast<const uint2*>(wsm + SM::kInBytes + ((r % SM::R) * 32 + lane) * 8);
+    };
+    auto u_row = [&](int i) -> uint32_t* {
+        return reinterpret_cast<uint32_t*>(wsm + SM::kUOff + (i * 32 + lane) * 16);
+    };
+    // In-plane terms of one level's plane: M = C | sx(C) | sy(C) [| sx(sy(C))],
+    // Z = C [| sx(sy(C))]: what the plane contributes to itself and to the
+    // planes above and below.
+    auto terms = [&](const uint32_t (&C)[NW], uint32_t (&M)[NW], uint32_t (&Z)[NW]) {
+        uint32_t Y[NW];
+#pragma unroll
+        for (int j = 0; j < NW; ++j) {
+            uint32_t up = __shfl_up_sync(kFull, C[j], 1);
+            uint32_t dn = __shfl_down_sync(kFull, C[j], 1);
+            if (lane == 0) up = 0u;
+            if (lane == 31) dn = 0u;
+            Y[j] = up | dn;
+        }
+#pragma unroll
+        for (int j = 0; j < NW; ++j) {
+            const uint32_t l = j > 0 ? C[j - 1] : 0u, r = j < NW - 1 ? C[j + 1] : 0u;
+            const uint32_t sx = (C[j] << 1) | (l >> 31) | (C[j] >> 1) | (r << 31);
+            if constexpr (!SE18) {
+                M[j] = C[j] | sx | Y[j];
+                Z[j] = C[j];
+            } else {
+                const uint32_t yl = j > 0 ? Y[j - 1] : 0u, yr = j < NW - 1 ? Y[j + 1] : 0u;
+                const uint32_t sxy = (Y[j] << 1) | (yl >> 31) | (Y[j] >> 1) | (yr << 31);
+                M[j] = C[j] | sx | Y[j] | sxy;
+                Z[j] = C[j] | sxy;
+            }
+        }
+    };
+
+    // Per level l < T: acc = M(p) | Z(p - 1) of the pending plane p and
+    // zp = Z(p); the next plane's terms complete plane p at level l + 1.
+    uint32_t acc[T][NW], zp[T][NW];
+    unsigned cnt[T];
+#pragma unroll
+    for (int s = 0; s < T; ++s) {
+        cnt[s] = 0;
+#pragma unroll
+        for (int j = 0; j < NW; ++j) acc[s][j] = zp[s][j] = 0u;
+    }
+    uint32_t d_any = 0, d_xl = 0, d_xh = 0, d_zl = 0, d_zh = 0, u_hits = 0;
+    const bool band_yl = inter && (lane - T) < T;
+    const bool band_yh = inter && (lane - T) >= BYI - T;
+    (void)p;
+
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+        // keep PF planes in flight, then wait for plane q (groups committed
+        // after it: planes q + 1 .. min(q + PF, NP - 1))
+        if (q + SM::PF < NP) tb_copy_plane<T, BZ>(w, q + SM::PF, wsm);
+        cp_async_wait_upto<SM::PF>((NP - 1 - q) < SM::PF ? (NP - 1 - q) : SM::PF);
+        // level 0: the loaded plane q
+        uint32_t M[NW], Z[NW];
+        {
+            const uint4 v = in_row(q);
+            const uint2 h = halo_row(q);
+            uint32_t C[NW] = {h.x & wm[0], v.x & wm[1], v.y & wm[2], v.z & wm[3], v.w & wm[4], h.y & wm[5]};
+            terms(C, M, Z);
+        }
+        // (M, Z) hold level s - 1 terms of plane q - s + 1: they complete
+        // plane r = q - s at level s
+#pragma unroll
+        for (int s = 1; s <= T; ++s) {
+            const int r = q - s;
+            uint32_t out[NW];
+#pragma unroll
+            for (int j = 0; j < NW; ++j) {
+                out[j] = acc[s - 1][j] | Z[j];
+                acc[s - 1][j] = M[j] | zp[s - 1][j];
+                zp[s - 1][j] = Z[j];
+            }
+            if (!(r >= s && r <= NP - 1 - s)) break;  // nothing complete at level s yet
+            const bool pv = plane_ok(r);
+#pragma unroll
+            for (int j = 0; j < NW; ++j) out[j] = pv ? (out[j] & wm[j]) : 0u;
+            if (r >= T && r < T + BZ) {
+                // cover test of the interior at step kb + s (U rows of
+                // non-interior lanes and planes are zero)
+                uint32_t* ur = u_row(r - T);
+                uint4 u = *reinterpret_cast<const uint4*>(ur);
+                const uint32_t h0 = out[1] & u.x, h1 = out[2] & u.y, h2 = out[3] & u.z, h3 = out[4] & u.w;
+                const uint32_t hany = h0 | h1 | h2 | h3;
+                if (hany) {
+                    cnt[s - 1] += __popc(h0) + __popc(h1) + __popc(h2) + __popc(h3);
+                    u.x &= ~h0;
+                    u.y &= ~h1;
+                    u.z &= ~h2;
+                    u.w &= ~h3;
+                    *reinterpret_cast<uint4*>(ur) = u;
+                    u_hits |= 1u << (r - T);
+                }
+            }
+            if (s < T) {
+                terms(out, M, Z);  // level s terms of plane r, for level s + 1
+            } else {
+                // final level: store, write back U, record changes
+                const int z = w.z0 - T + r;
+                if (inter && z < w.Dd) {
+                    const int off = z * w.plane + w.rowoff;
+                    *reinterpret_cast<uint4*>(dst + off) = make_uint4(out[1], out[2], out[3], out[4]);
+                    const uint4 c0 = in_row(r);
+                    const uint32_t dx0 = out[1] ^ (c0.x & wm[1]), dx3 = out[4] ^ (c0.w & wm[4]);
+                    const uint32_t dall = dx0 | (out[2] ^ (c0.y & wm[2])) | (out[3] ^ (c0.z & wm[3])) | dx3;
+                    // only changes within T voxels of an x face can reach
+                    // the x neighbour's interior during its next T steps
+                    constexpr uint32_t kLoBits = (1u << T) - 1u, kHiBits = ~(0xffffffffu >> T);
+                    if (u_hits & (1u << (r - T)))
+                        *reinterpret_cast<uint4*>(U + off) = *reinterpret_cast<const uint4*>(u_row(r - T));
+                    d_any |= dall;
+                    d_xl |= dx0 & kLoBits;
+                    d_xh |= dx3 & kHiBits;
+                    if (r - T < T) d_zl |= dall;
+                    if (r - T >= BZ - T) d_zh |= dall;
+                }
+            }
+        }
+    }
+
+    // per-step hit counts and frontier flags
+#pragma unroll
+    for (int s = 0; s < T; ++s) {
+        unsigned c = cnt[s];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+        res.cnt[s] = c;
+    }
+    res.any = __any_sync(kFull, d_any != 0);
+    res.fxl = __any_sync(kFull, d_xl != 0);
+    res.fxh = __any_sync(kFull, d_xh != 0);
+    res.fyl = __any_sync(kFull, band_yl && d_any != 0);
+    res.fyh = __any_sync(kFull, band_yh && d_any != 0);
+    res.fzl = __any_sync(kFull, d_zl != 0);
+    res.fzh = __any_sync(kFull, d_zh != 0);
+}
+
+// Staging chosen by T (see tb_all_planes).
+template <int T, int BZ>
+__device__ __forceinline__ void tb_issue(const SolveParams& p, unsigned long long e, int g, unsigned char* wsm,
+                                         TbItem& it) {
+    if constexpr (tb_all_planes(T)) tb_issue_all<T, BZ>(p, e, g, wsm, it);
+    else tb_issue_ring<T, BZ>(p, e, g, wsm, it);
+}
+template <int T, int BZ, bool SE18>
+__device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& it, unsigned char* wsm, TbOut& res) {
+    if constexpr (tb_all_planes(T)) tb_compute_all<T, BZ, SE18>(p, it, wsm, res);
+    else tb_compute_ring<T, BZ, SE18>(p, it, wsm, res);
+}
+
 // Counts, frontier, completion.  The completion atomic's return value is
 // consumed last, so its latency overlaps the frontier atomics.
 template <int T, bool SE18>
@@ -372,10 +691,8 @@ __device__ __forceinline__ void tb_epilogue(const SolveParams& p, const TbItem& 
     }
 }
 
-constexpr int kTbWarps = 4;  // warps per CTA of the blocked kernel
-
 template <int T, int BZ, bool SE18>
-__global__ void __launch_bounds__(kTbWarps * 32) solve_tb_kernel(SolveParams p) {
+__global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel(SolveParams p) {
     extern __shared__ __align__(16) unsigned char tb_smem[];
     __shared__ int s_flag;
     __shared__ unsigned s_gen, s_cnt;
@@ -392,7 +709,7 @@ __global__ void __launch_bounds__(kTbWarps * 32) solve_tb_kernel(SolveParams p) 
     const unsigned nw = gridDim.x * wpb;
     int g = p.g0;
     int it = 0;
-    unsigned char* wsm = tb_smem + (threadIdx.x >> 5) * TbSmem<T, BZ>::kWarpBytes;
+    unsigned char* wsm = tb_smem + (threadIdx.x >> 5) * tb_warp_bytes(T, BZ);
     if (cnt > 0) {
         for (;;) {
             const int qi = g % 3;
