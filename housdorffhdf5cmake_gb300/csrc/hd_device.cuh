@@ -126,15 +126,17 @@ struct JobState {
 
 // Loop control shared by all CTAs of the persistent kernel.
 struct Ctl {
+    // barrier release word, written once per barrier by the last CTA to
+    // arrive: generation (bits 32-63) | continue flag (bit 31) | length of
+    // the next step's queue (bits 0-30)
+    unsigned long long release;
     unsigned int bar_count;
-    unsigned int bar_gen;
     int32_t err;           // first error (hd_status), 0 = none
     int32_t jobs_active;   // jobs with uncovered target voxels
     unsigned int qcount[3];
-    int32_t cont[2];       // continue flag decided by the last CTA at each barrier (by parity)
     int32_t g_end;         // next global iteration (written at exit)
     int32_t iters_run;
-    int32_t pad[5];
+    int32_t pad[6];
 };
 
 struct SolveParams {

@@ -41,6 +41,11 @@ __device__ __forceinline__ int ld_relaxed_s32(const int* p) {
     asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
     unsigned v;
     asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -61,11 +66,12 @@ constexpr int kErrIterLimit = 7;  // HD_ERR_ITER_LIMIT
 // the others.  Every wait is bounded: after timeout_ns (or 2^26 polls) the
 // waiting CTA records HD_ERR_TIMEOUT and leaves, and every other waiter sees
 // the error and leaves as well.  Returns the continue flag (CTA-uniform).
-__device__ __forceinline__ bool grid_step_barrier(Ctl* ctl, unsigned& gen, int g,
-                                                  long long timeout_ns, int* s_flag) {
+__device__ __forceinline__ bool grid_step_barrier(Ctl* ctl, unsigned& gen, int g, long long timeout_ns, int* s_flag,
+                                                  unsigned* s_cnt) {
     __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned target = gen + 1u;
+        unsigned long long rel = 0ull;
         __threadfence();
         const unsigned arrived = atomicAdd(&ctl->bar_count, 1u);
         if (arrived == gridDim.x - 1u) {
@@ -74,29 +80,31 @@ __device__ __forceinline__ bool grid_step_barrier(Ctl* ctl, unsigned& gen, int g
             const int err = ld_relaxed_s32(&ctl->err);
             const int jobs = ld_relaxed_s32(&ctl->jobs_active);
             const unsigned nq = ld_relaxed_u32(&ctl->qcount[(g + 1) % 3]);
-            ctl->cont[target & 1u] = (err == 0 && jobs > 0 && nq > 0u) ? 1 : 0;
+            const bool cont = err == 0 && jobs > 0 && nq > 0u;
             ctl->qcount[(g + 2) % 3] = 0u;
+            rel = ((unsigned long long)target << 32) | (cont ? 0x80000000ull : 0ull) | (nq & 0x7fffffffu);
             __threadfence();
-            atomicExch(&ctl->bar_gen, target);
+            atomicExch(&ctl->release, rel);
         } else {
+            // poll hot at first (a barrier normally completes within a few
+            // microseconds), then with short sleeps; bounded in time and count
             const unsigned long long t0 = globaltimer_ns();
-            unsigned sleep_ns = 32;
             unsigned polls = 0;
-            while (ld_acquire_u32(&ctl->bar_gen) != target) {
+            for (;;) {
+                rel = ld_acquire_u64(&ctl->release);
+                if ((unsigned)(rel >> 32) == target) break;
                 if (ld_relaxed_s32(&ctl->err) != 0) break;
-                __nanosleep(sleep_ns);
-                if (sleep_ns < 512) sleep_ns <<= 1;
-                ++polls;
+                if (++polls > 64u) __nanosleep(64);
                 if ((long long)(globaltimer_ns() - t0) > timeout_ns || polls > (1u << 26)) {
                     atomicCAS(&ctl->err, 0, kErrTimeout);
                     break;
                 }
             }
         }
-        __threadfence();
-        const int cont = ld_relaxed_s32(&ctl->cont[target & 1u]);
-        const int err = ld_relaxed_s32(&ctl->err);
-        *s_flag = (cont != 0 && err == 0) ? 1 : 0;
+        // the release word carries the decision: no further load
+        const bool released = (unsigned)(rel >> 32) == target;
+        *s_flag = (released && (rel & 0x80000000ull)) ? 1 : 0;
+        *s_cnt = (unsigned)(rel & 0x7fffffffull);
     }
     gen += 1u;
     __syncthreads();
@@ -328,7 +336,7 @@ __global__ void __launch_bounds__(256, 2) solve_kernel(SolveParams p) {
     __shared__ unsigned s_gen, s_cnt;
     Ctl* ctl = p.ctl;
     if (threadIdx.x == 0) {
-        s_gen = ld_acquire_u32(&ctl->bar_gen);
+        s_gen = (unsigned)(ld_acquire_u64(&ctl->release) >> 32);
         s_cnt = ld_relaxed_u32(&ctl->qcount[p.g0 % 3]);  // global memory: dynamic index is fine
     }
     __syncthreads();
@@ -347,13 +355,11 @@ __global__ void __launch_bounds__(256, 2) solve_kernel(SolveParams p) {
                 const unsigned long long e = Q[i];
                 brick_step<BXW, BZ, SE18>(p, (int)((e >> 32) & 0xffffffu), (unsigned)e, (unsigned)(e >> 56), g);
             }
-            const bool cont = grid_step_barrier(ctl, gen, g, p.timeout_ns, &s_flag);
+            const bool cont = grid_step_barrier(ctl, gen, g, p.timeout_ns, &s_flag, &s_cnt);
             ++g;
             ++it;
             if (!cont || it >= p.max_iters) break;
-            if (threadIdx.x == 0) s_cnt = ld_relaxed_u32(&ctl->qcount[g % 3]);
-            __syncthreads();
-            cnt = s_cnt;
+            cnt = s_cnt;  // the next queue's length, published by the barrier
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {

@@ -101,6 +101,7 @@ struct TbItem {
     unsigned lb;
     int iter, kb;
     int bx, by, bz;
+    int active;  // the job's active flag as loaded at issue (checked when the item is computed)
     bool live;
 };
 
@@ -151,6 +152,47 @@ __device__ __forceinline__ void tb_copy_plane(const TbRow& w, int r, unsigned ch
     cp_async_commit();
 }
 
+// Decodes a queue entry and decides whether the item runs (its job still
+// needs work, the entry is not left over from a slot's previous pair, the
+// step cap is not passed).  The job state and every job field the item reads
+// are loaded in one batch, so their latencies overlap.
+template <int T>
+__device__ __forceinline__ bool tb_decode(const SolveParams& p, unsigned long long e, int g, TbItem& it) {
+    const int lane = threadIdx.x & 31;
+    it.jid = (int)((e >> 32) & 0xffffffu);
+    it.lb = (unsigned)e;
+    it.epoch = (unsigned)(e >> 56);
+    it.st = p.states + it.jid;
+    it.Jp = p.jobs + it.jid;
+    it.live = false;
+    const Job* Jp = it.Jp;
+    // the job's active flag is only needed when the item is computed: the
+    // copies do not wait for it (an item of a job that finished meanwhile is
+    // dropped then, after its copies have landed)
+    it.active = ld_relaxed_s32(&it.st->active);
+    const uint32_t jep = Jp->epoch;
+    const int k0 = Jp->k0, kmax = Jp->kmax, nbx = Jp->nbx, nby = Jp->nby;
+    // touched here so that the issue and compute phases find them in L1
+    const int warm = Jp->wx + Jp->h + Jp->d + Jp->pitch + (int)Jp->tailmask;
+    asm volatile("" ::"r"(warm));
+    if ((jep & 0xffu) != it.epoch) return false;  // left over from the slot's previous pair
+    it.iter = g - k0;
+    it.kb = it.iter * T;
+    if (it.kb + 1 > kmax) {
+        if (lane == 0) {
+            it.st->status = kErrIterLimit;
+            atomicCAS(&p.ctl->err, 0, kErrIterLimit);
+        }
+        return false;
+    }
+    it.bx = (int)(it.lb % (unsigned)nbx);
+    const unsigned tq = it.lb / (unsigned)nbx;
+    it.by = (int)(tq % (unsigned)nby);
+    it.bz = (int)(tq / (unsigned)nby);
+    it.live = true;
+    return true;
+}
+
 // All-planes staging: decodes a queue entry, checks that its job still needs
 // work, and issues every copy of the brick into the warp's shared memory
 // (rows, planes and halo words outside the domain are zero-filled) as one
@@ -163,30 +205,8 @@ __device__ __forceinline__ void tb_issue_all(const SolveParams& p, unsigned long
     constexpr int NP = BZ + 2 * T;
     using SM = TbSmemAll<T, BZ>;
     const int lane = threadIdx.x & 31;
-    it.jid = (int)((e >> 32) & 0xffffffu);
-    it.lb = (unsigned)e;
-    it.epoch = (unsigned)(e >> 56);
-    it.st = p.states + it.jid;
-    it.Jp = p.jobs + it.jid;
-    it.live = false;
-    if (ld_relaxed_s32(&it.st->active) == 0) return;     // nothing left to cover
+    if (!tb_decode<T>(p, e, g, it)) return;
     const Job* Jp = it.Jp;
-    if ((Jp->epoch & 0xffu) != it.epoch) return;         // left over from the slot's previous pair
-    it.iter = g - Jp->k0;
-    it.kb = it.iter * T;
-    if (it.kb + 1 > Jp->kmax) {
-        if (lane == 0) {
-            it.st->status = kErrIterLimit;
-            atomicCAS(&p.ctl->err, 0, kErrIterLimit);
-        }
-        return;
-    }
-    const int nbx = Jp->nbx, nby = Jp->nby;
-    it.bx = (int)(it.lb % (unsigned)nbx);
-    const unsigned tq = it.lb / (unsigned)nbx;
-    it.by = (int)(tq % (unsigned)nby);
-    it.bz = (int)(tq / (unsigned)nby);
-    it.live = true;
     const int Wx = Jp->wx, Hd = Jp->h, Dd = Jp->d;
     const int wx0 = it.bx * IW, z0 = it.bz * BZ;
     const int y = it.by * BYI - T + lane;
@@ -229,30 +249,8 @@ __device__ __forceinline__ void tb_issue_ring(const SolveParams& p, unsigned lon
                                          TbItem& it) {
     using SM = TbSmemRing<T, BZ>;
     const int lane = threadIdx.x & 31;
-    it.jid = (int)((e >> 32) & 0xffffffu);
-    it.lb = (unsigned)e;
-    it.epoch = (unsigned)(e >> 56);
-    it.st = p.states + it.jid;
-    it.Jp = p.jobs + it.jid;
-    it.live = false;
-    if (ld_relaxed_s32(&it.st->active) == 0) return;     // nothing left to cover
+    if (!tb_decode<T>(p, e, g, it)) return;
     const Job* Jp = it.Jp;
-    if ((Jp->epoch & 0xffu) != it.epoch) return;         // left over from the slot's previous pair
-    it.iter = g - Jp->k0;
-    it.kb = it.iter * T;
-    if (it.kb + 1 > Jp->kmax) {
-        if (lane == 0) {
-            it.st->status = kErrIterLimit;
-            atomicCAS(&p.ctl->err, 0, kErrIterLimit);
-        }
-        return;
-    }
-    const int nbx = Jp->nbx, nby = Jp->nby;
-    it.bx = (int)(it.lb % (unsigned)nbx);
-    const unsigned tq = it.lb / (unsigned)nbx;
-    it.by = (int)(tq % (unsigned)nby);
-    it.bz = (int)(tq / (unsigned)nby);
-    it.live = true;
     const TbRow w = tb_row<T, BZ>(it);
     const bool inter = w.rowv && lane >= T && lane < 32 - T;
     const uint32_t s_u = (uint32_t)__cvta_generic_to_shared(wsm) + SM::kUOff;
@@ -272,6 +270,7 @@ constexpr int kTbMaxSteps = 4;
 struct TbOut {
     unsigned cnt[kTbMaxSteps];  // newly covered voxels per step of the item
     bool any, fxl, fxh, fyl, fyh, fzl, fzh;
+    bool skip;                  // the job had finished: nothing computed, no epilogue
 };
 
 // All-planes staging: waits for the item's copies, runs its T steps (per
@@ -287,6 +286,11 @@ __device__ __forceinline__ void tb_compute_all(const SolveParams& p, const TbIte
     using SM = TbSmemAll<T, BZ>;
     const int lane = threadIdx.x & 31;
     const Job* Jp = it.Jp;
+    res.skip = it.active == 0;
+    if (res.skip) {  // job finished: let the item's copies land (the buffer is reused next) and drop it
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        return;
+    }
     const int Wx = Jp->wx, Hd = Jp->h, Dd = Jp->d;
     const int wx0 = it.bx * IW, z0 = it.bz * BZ;
     const int y = it.by * BYI - T + lane;
@@ -459,6 +463,11 @@ __device__ __forceinline__ void tb_compute_ring(const SolveParams& p, const TbIt
     constexpr int NP = SM::NP;
     const int lane = threadIdx.x & 31;
     const Job* Jp = it.Jp;
+    res.skip = it.active == 0;
+    if (res.skip) {  // job finished: let the item's copies land (the ring is reused next) and drop it
+        cp_async_wait<0>();
+        return;
+    }
     const TbRow w = tb_row<T, BZ>(it);
     const int Wx = Jp->wx;
     const int wx0 = it.bx * IW;
@@ -636,6 +645,7 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
 // consumed last, so its latency overlaps the frontier atomics.
 template <int T, bool SE18>
 __device__ __forceinline__ void tb_epilogue(const SolveParams& p, const TbItem& it, const TbOut& res, int g) {
+    if (res.skip) return;
     const int lane = threadIdx.x & 31;
     const Job* Jp = it.Jp;
     JobState* st = it.st;
@@ -698,7 +708,7 @@ __global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel
     __shared__ unsigned s_gen, s_cnt;
     Ctl* ctl = p.ctl;
     if (threadIdx.x == 0) {
-        s_gen = ld_acquire_u32(&ctl->bar_gen);
+        s_gen = (unsigned)(ld_acquire_u64(&ctl->release) >> 32);
         s_cnt = ld_relaxed_u32(&ctl->qcount[p.g0 % 3]);
     }
     __syncthreads();
@@ -732,13 +742,11 @@ __global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel
                 cur = nxt;
                 i = in;
             }
-            const bool cont = grid_step_barrier(ctl, gen, g, p.timeout_ns, &s_flag);
+            const bool cont = grid_step_barrier(ctl, gen, g, p.timeout_ns, &s_flag, &s_cnt);
             ++g;
             ++it;
             if (!cont || it >= p.max_iters) break;
-            if (threadIdx.x == 0) s_cnt = ld_relaxed_u32(&ctl->qcount[g % 3]);
-            __syncthreads();
-            cnt = s_cnt;
+            cnt = s_cnt;  // the next queue's length, published by the barrier
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
