@@ -134,11 +134,16 @@ __device__ __forceinline__ void flush_acc(const PairDesc& P, const PackAcc& acc)
 }
 
 // Nonzero bytes among the 16 at p that lie inside [lo, hi), as 16 bits (a
-// mask's first and last 16-byte chunks may stick out of it).
+// mask's first and last 16-byte chunks may stick out of it).  The byte loads
+// are predicated, not branched over, so all sixteen are in flight together.
 __device__ __noinline__ uint32_t chunk_bits_edge(const uint8_t* p, const uint8_t* lo, const uint8_t* hi) {
     uint32_t bits = 0;
-    for (int i = 0; i < 16; ++i)
-        if (p + i >= lo && p + i < hi && p[i] != 0) bits |= 1u << i;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const bool in = p + i >= lo && p + i < hi;
+        const uint8_t v = in ? __ldg(p + i) : (uint8_t)0;
+        bits |= (v != 0 ? 1u : 0u) << i;
+    }
     return bits;
 }
 
