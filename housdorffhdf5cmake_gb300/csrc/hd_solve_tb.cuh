@@ -335,25 +335,22 @@ __device__ __forceinline__ void tb_compute_all(const SolveParams& p, const TbIte
     // Z = C [| sx(sy(C))]: what the plane contributes to itself and to the
     // planes above and below.
     auto terms = [&](const uint32_t (&C)[NW], uint32_t (&M)[NW], uint32_t (&Z)[NW]) {
+        // rows: lanes 0 and 31 get their own row back from the shuffle,
+        // which is already in M, the same as an empty row outside
         uint32_t Y[NW];
 #pragma unroll
-        for (int j = 0; j < NW; ++j) {
-            uint32_t up = __shfl_up_sync(kFull, C[j], 1);
-            uint32_t dn = __shfl_down_sync(kFull, C[j], 1);
-            if (lane == 0) up = 0u;
-            if (lane == 31) dn = 0u;
-            Y[j] = up | dn;
-        }
+        for (int j = 0; j < NW; ++j) Y[j] = __shfl_up_sync(kFull, C[j], 1) | __shfl_down_sync(kFull, C[j], 1);
+        // x: one funnel shift per direction carries the neighbour word's bit
 #pragma unroll
         for (int j = 0; j < NW; ++j) {
             const uint32_t l = j > 0 ? C[j - 1] : 0u, r = j < NW - 1 ? C[j + 1] : 0u;
-            const uint32_t sx = (C[j] << 1) | (l >> 31) | (C[j] >> 1) | (r << 31);
+            const uint32_t sx = __funnelshift_l(l, C[j], 1) | __funnelshift_r(C[j], r, 1);
             if constexpr (!SE18) {
                 M[j] = C[j] | sx | Y[j];
                 Z[j] = C[j];
             } else {
                 const uint32_t yl = j > 0 ? Y[j - 1] : 0u, yr = j < NW - 1 ? Y[j + 1] : 0u;
-                const uint32_t sxy = (Y[j] << 1) | (yl >> 31) | (Y[j] >> 1) | (yr << 31);
+                const uint32_t sxy = __funnelshift_l(yl, Y[j], 1) | __funnelshift_r(Y[j], yr, 1);
                 M[j] = C[j] | sx | Y[j] | sxy;
                 Z[j] = C[j] | sxy;
             }
@@ -498,25 +495,22 @@ __device__ __forceinline__ void tb_compute_ring(const SolveParams& p, const TbIt
     // Z = C [| sx(sy(C))]: what the plane contributes to itself and to the
     // planes above and below.
     auto terms = [&](const uint32_t (&C)[NW], uint32_t (&M)[NW], uint32_t (&Z)[NW]) {
+        // rows: lanes 0 and 31 get their own row back from the shuffle,
+        // which is already in M, the same as an empty row outside
         uint32_t Y[NW];
 #pragma unroll
-        for (int j = 0; j < NW; ++j) {
-            uint32_t up = __shfl_up_sync(kFull, C[j], 1);
-            uint32_t dn = __shfl_down_sync(kFull, C[j], 1);
-            if (lane == 0) up = 0u;
-            if (lane == 31) dn = 0u;
-            Y[j] = up | dn;
-        }
+        for (int j = 0; j < NW; ++j) Y[j] = __shfl_up_sync(kFull, C[j], 1) | __shfl_down_sync(kFull, C[j], 1);
+        // x: one funnel shift per direction carries the neighbour word's bit
 #pragma unroll
         for (int j = 0; j < NW; ++j) {
             const uint32_t l = j > 0 ? C[j - 1] : 0u, r = j < NW - 1 ? C[j + 1] : 0u;
-            const uint32_t sx = (C[j] << 1) | (l >> 31) | (C[j] >> 1) | (r << 31);
+            const uint32_t sx = __funnelshift_l(l, C[j], 1) | __funnelshift_r(C[j], r, 1);
             if constexpr (!SE18) {
                 M[j] = C[j] | sx | Y[j];
                 Z[j] = C[j];
             } else {
                 const uint32_t yl = j > 0 ? Y[j - 1] : 0u, yr = j < NW - 1 ? Y[j + 1] : 0u;
-                const uint32_t sxy = (Y[j] << 1) | (yl >> 31) | (Y[j] >> 1) | (yr << 31);
+                const uint32_t sxy = __funnelshift_l(yl, Y[j], 1) | __funnelshift_r(Y[j], yr, 1);
                 M[j] = C[j] | sx | Y[j] | sxy;
                 Z[j] = C[j] | sxy;
             }
