@@ -280,7 +280,7 @@ template <int T, int BZ, bool SE18>
 __device__ __forceinline__ void tb_compute_all(const SolveParams& p, const TbItem& it, unsigned char* wsm, TbOut& res) {
     static_assert(T >= 1 && T <= kTbMaxSteps, "steps per barrier out of range");
     constexpr int IW = 4;
-    constexpr int NW = IW + 2;
+    constexpr int NW = IW + 1;  // [combined halo word, 4 interior words]
     constexpr int BYI = 32 - 2 * T;
     constexpr int NP = BZ + 2 * T;
     using SM = TbSmemAll<T, BZ>;
@@ -303,10 +303,16 @@ __device__ __forceinline__ void tb_compute_all(const SolveParams& p, const TbIte
     const int rowoff = (rowv ? y : 0) * pitch + wx0;
     const int kb = it.kb;
     uint32_t wm[NW];  // valid bits of each word of this lane's row
+    {
+        uint32_t w6[IW + 2];
 #pragma unroll
-    for (int j = 0; j < NW; ++j) {
-        const int w = wx0 - 1 + j;
-        wm[j] = (rowv && w >= 0 && w < Wx) ? (w == Wx - 1 ? Jp->tailmask : kFull) : 0u;
+        for (int j = 0; j < IW + 2; ++j) {
+            const int w = wx0 - 1 + j;
+            w6[j] = (rowv && w >= 0 && w < Wx) ? (w == Wx - 1 ? Jp->tailmask : kFull) : 0u;
+        }
+        wm[0] = (w6[0] & 0xffff0000u) | (w6[IW + 1] & 0x0000ffffu);
+#pragma unroll
+        for (int j = 1; j <= IW; ++j) wm[j] = w6[j];
     }
     asm volatile("cp.async.wait_group 0;" ::: "memory");  // each lane reads back only its own rows
 
@@ -324,12 +330,11 @@ __device__ __forceinline__ void tb_compute_all(const SolveParams& p, const TbIte
         const uint32_t* rp = in_row(r);
         const uint4 v = *reinterpret_cast<const uint4*>(rp);
         const uint2 h = *reinterpret_cast<const uint2*>(rp + 4);
-        C[0] = h.x & wm[0];
+        C[0] = ((h.x & 0xffff0000u) | (h.y & 0x0000ffffu)) & wm[0];
         C[1] = v.x & wm[1];
         C[2] = v.y & wm[2];
         C[3] = v.z & wm[3];
         C[4] = v.w & wm[4];
-        C[5] = h.y & wm[5];
     };
     // In-plane terms of one level's plane: M = C | sx(C) | sy(C) [| sx(sy(C))],
     // Z = C [| sx(sy(C))]: what the plane contributes to itself and to the
@@ -340,16 +345,22 @@ __device__ __forceinline__ void tb_compute_all(const SolveParams& p, const TbIte
         uint32_t Y[NW];
 #pragma unroll
         for (int j = 0; j < NW; ++j) Y[j] = __shfl_up_sync(kFull, C[j], 1) | __shfl_down_sync(kFull, C[j], 1);
-        // x: one funnel shift per direction carries the neighbour word's bit
+        // x: one funnel shift per direction carries the neighbour word's
+        // bit.  The words form a ring [H, I0, I1, I2, I3]: the halo word H
+        // holds the left neighbour word's high half (x0 - 16 .. x0 - 1) in
+        // bits 16-31 and the right neighbour word's low half (x1 + 1 ..
+        // x1 + 16) in bits 0-15, so I3 is H's left and I0 its right
+        // neighbour; the two halves trade bits 15 and 16, 16 voxels from the
+        // interior, which T <= 4 steps never carry back
 #pragma unroll
         for (int j = 0; j < NW; ++j) {
-            const uint32_t l = j > 0 ? C[j - 1] : 0u, r = j < NW - 1 ? C[j + 1] : 0u;
+            const uint32_t l = C[(j + NW - 1) % NW], r = C[(j + 1) % NW];
             const uint32_t sx = __funnelshift_l(l, C[j], 1) | __funnelshift_r(C[j], r, 1);
             if constexpr (!SE18) {
                 M[j] = C[j] | sx | Y[j];
                 Z[j] = C[j];
             } else {
-                const uint32_t yl = j > 0 ? Y[j - 1] : 0u, yr = j < NW - 1 ? Y[j + 1] : 0u;
+                const uint32_t yl = Y[(j + NW - 1) % NW], yr = Y[(j + 1) % NW];
                 const uint32_t sxy = __funnelshift_l(yl, Y[j], 1) | __funnelshift_r(Y[j], yr, 1);
                 M[j] = C[j] | sx | Y[j] | sxy;
                 Z[j] = C[j] | sxy;
@@ -454,7 +465,7 @@ template <int T, int BZ, bool SE18>
 __device__ __forceinline__ void tb_compute_ring(const SolveParams& p, const TbItem& it, unsigned char* wsm, TbOut& res) {
     static_assert(T >= 1 && T <= kTbMaxSteps, "steps per barrier out of range");
     constexpr int IW = 4;
-    constexpr int NW = IW + 2;
+    constexpr int NW = IW + 1;  // [combined halo word, 4 interior words]
     constexpr int BYI = 32 - 2 * T;
     using SM = TbSmemRing<T, BZ>;
     constexpr int NP = SM::NP;
@@ -472,10 +483,16 @@ __device__ __forceinline__ void tb_compute_ring(const SolveParams& p, const TbIt
     uint32_t* __restrict__ dst = Jp->buf[(it.iter + 1) & 1];
     uint32_t* __restrict__ U = Jp->U;
     uint32_t wm[NW];  // valid bits of each word of this lane's row
+    {
+        uint32_t w6[IW + 2];
 #pragma unroll
-    for (int j = 0; j < NW; ++j) {
-        const int x = wx0 - 1 + j;
-        wm[j] = (w.rowv && x >= 0 && x < Wx) ? (x == Wx - 1 ? Jp->tailmask : kFull) : 0u;
+        for (int j = 0; j < IW + 2; ++j) {
+            const int x = wx0 - 1 + j;
+            w6[j] = (w.rowv && x >= 0 && x < Wx) ? (x == Wx - 1 ? Jp->tailmask : kFull) : 0u;
+        }
+        wm[0] = (w6[0] & 0xffff0000u) | (w6[IW + 1] & 0x0000ffffu);
+#pragma unroll
+        for (int j = 1; j <= IW; ++j) wm[j] = w6[j];
     }
 
     auto plane_ok = [&](int r) {  // streamed plane index r -> inside the domain
@@ -500,16 +517,22 @@ __device__ __forceinline__ void tb_compute_ring(const SolveParams& p, const TbIt
         uint32_t Y[NW];
 #pragma unroll
         for (int j = 0; j < NW; ++j) Y[j] = __shfl_up_sync(kFull, C[j], 1) | __shfl_down_sync(kFull, C[j], 1);
-        // x: one funnel shift per direction carries the neighbour word's bit
+        // x: one funnel shift per direction carries the neighbour word's
+        // bit.  The words form a ring [H, I0, I1, I2, I3]: the halo word H
+        // holds the left neighbour word's high half (x0 - 16 .. x0 - 1) in
+        // bits 16-31 and the right neighbour word's low half (x1 + 1 ..
+        // x1 + 16) in bits 0-15, so I3 is H's left and I0 its right
+        // neighbour; the two halves trade bits 15 and 16, 16 voxels from the
+        // interior, which T <= 4 steps never carry back
 #pragma unroll
         for (int j = 0; j < NW; ++j) {
-            const uint32_t l = j > 0 ? C[j - 1] : 0u, r = j < NW - 1 ? C[j + 1] : 0u;
+            const uint32_t l = C[(j + NW - 1) % NW], r = C[(j + 1) % NW];
             const uint32_t sx = __funnelshift_l(l, C[j], 1) | __funnelshift_r(C[j], r, 1);
             if constexpr (!SE18) {
                 M[j] = C[j] | sx | Y[j];
                 Z[j] = C[j];
             } else {
-                const uint32_t yl = j > 0 ? Y[j - 1] : 0u, yr = j < NW - 1 ? Y[j + 1] : 0u;
+                const uint32_t yl = Y[(j + NW - 1) % NW], yr = Y[(j + 1) % NW];
                 const uint32_t sxy = __funnelshift_l(yl, Y[j], 1) | __funnelshift_r(Y[j], yr, 1);
                 M[j] = C[j] | sx | Y[j] | sxy;
                 Z[j] = C[j] | sxy;
@@ -543,7 +566,8 @@ __device__ __forceinline__ void tb_compute_ring(const SolveParams& p, const TbIt
         {
             const uint4 v = in_row(q);
             const uint2 h = halo_row(q);
-            uint32_t C[NW] = {h.x & wm[0], v.x & wm[1], v.y & wm[2], v.z & wm[3], v.w & wm[4], h.y & wm[5]};
+            uint32_t C[NW] = {((h.x & 0xffff0000u) | (h.y & 0x0000ffffu)) & wm[0], v.x & wm[1], v.y & wm[2],
+                              v.z & wm[3], v.w & wm[4]};
             terms(C, M, Z);
         }
         // (M, Z) hold level s - 1 terms of plane q - s + 1: they complete
