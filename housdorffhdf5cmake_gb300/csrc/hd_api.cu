@@ -220,14 +220,12 @@ hd_status decode_result(const hdk::PairInfo& I, const hdk::JobState& s0, const h
 Shape pick_shape(hd_context* ctx, int se, const PairIn* pairs, int n) {
     // built-in default (the autotuner's winners on GB300): the blocked kernel
     // with 4 x (32 - 2 steps) x 8 bricks; 4 steps per barrier for a single
-    // pair (fewest barriers), 3 for a single pair of 100 M voxels or more
-    // (its bricks outnumber the warps: the ring-staged kernel's third CTA per
-    // SM pays), 2 for batches (the work per barrier is large)
+    // pair (fewest barriers), 2 for batches (the work per barrier is large)
     Shape sh;
     double vox = 0;
     for (int i = 0; i < n; ++i) vox += (double)pairs[i].W * pairs[i].H * pairs[i].D;
     vox /= std::max(1, n);
-    sh.steps = n <= 1 ? (vox >= 100e6 ? 3 : 4) : 2;
+    sh.steps = n <= 1 ? 4 : 2;
     auto it = ctx->tune.entries.find(tune_key(se, vox, n));
     if (it != ctx->tune.entries.end()) sh = it->second.shape;
     const hd_options& o = ctx->opt;

@@ -59,26 +59,21 @@ struct PairDesc {
 // to 4 words: roundup(wxf, 4) * H * D).
 constexpr long long kTileWords = 1024;
 
-// Temporally blocked dilation kernel (hd_solve_tb.cuh).  Each warp streams
-// the BZ + 2T planes of its brick through shared memory.  With 4 steps per
-// barrier all planes are copied when the item is issued (rows of 32 B; 2
-// CTAs per SM; shortest item latency, best when a launch has few bricks per
-// warp).  With fewer steps the planes go through a ring kTbPrefetch planes
-// ahead of the one being computed (rows of 24 B; a plane stays until its
-// final step has been compared with it, T planes later), which leaves room
-// for a third CTA per SM (best when bricks outnumber warps).  Both keep the
-// brick's uncovered-target rows (BZ planes x 32 rows x 16 B).
+// Temporally blocked dilation kernel (hd_solve_tb.cuh): each warp streams
+// the BZ + 2T planes of its brick through a ring of shared-memory slots
+// kTbPrefetch planes ahead of the one being computed; a plane stays until
+// its final step has been compared with it, T planes later.  Per warp: the
+// slots (32 rows x (16 B interior + 8 B halo words)) and the brick's
+// uncovered-target rows (BZ planes x 32 rows x 16 B).  3 CTAs of kTbWarps
+// warps fit on an SM.
 constexpr int kTbWarps = 4;
 constexpr int kTbPrefetch = 3;
-__host__ __device__ constexpr bool tb_all_planes(int T) { return T >= 4; }
-__host__ __device__ constexpr int tb_prefetch(int T, int BZ) { return tb_all_planes(T) ? BZ + 2 * T : kTbPrefetch; }
+constexpr int kTbMinCtas = 3;
 __host__ __device__ constexpr int tb_ring_slots(int T, int BZ) {
-    return (tb_all_planes(T) || T + 1 + kTbPrefetch >= BZ + 2 * T) ? BZ + 2 * T : T + 1 + kTbPrefetch;
+    return T + 1 + kTbPrefetch >= BZ + 2 * T ? BZ + 2 * T : T + 1 + kTbPrefetch;
 }
-__host__ __device__ constexpr int tb_min_ctas(int T) { return tb_all_planes(T) ? 2 : 3; }
 __host__ __device__ constexpr int tb_warp_bytes(int T, int BZ) {
-    return tb_all_planes(T) ? (BZ + 2 * T) * 32 * 32 + BZ * 32 * 16   // rows padded to 32 B
-                            : tb_ring_slots(T, BZ) * 32 * 24 + BZ * 32 * 16;
+    return tb_ring_slots(T, BZ) * 32 * 24 + BZ * 32 * 16;
 }
 __host__ __device__ __forceinline__ long long pack_words(int W, int H, int D) {
     return (long long)((W + 31) / 32) * H * D;

@@ -5,26 +5,24 @@
 // hd_solve.cuh, but one queue item advances a brick by T dilation steps:
 //
 //   brick     IW = 4 words (128 voxels) in x  x  32 - 2T rows  x  BZ planes
-//   warp      lane = one row: the 4 interior words plus one halo word on
-//             each side, rows y0 - T .. y0 + 32 - T - 1 (T halo rows above
-//             and below the interior), streamed plane by plane along z from
-//             z0 - T to z0 + BZ + T - 1
+//   warp      lane = one row: the 4 interior words plus one halo word
+//             holding the 16 voxels on each side of them, rows y0 - T ..
+//             y0 + 32 - T - 1 (T halo rows above and below the interior),
+//             streamed plane by plane along z from z0 - T to z0 + BZ + T - 1
 //   levels    level 0 is the loaded state; level s is the state after s
 //             steps, computed one plane behind level s - 1 from three of its
 //             planes; rows come from the neighbouring lanes by shuffle, x
 //             carries from the neighbouring words of the row
-//   staging   planes arrive by cp.async (zero fill outside the domain).  With
-//             T = 4 every plane is copied when the item is issued, before
-//             the previous item's epilogue (shortest item latency; 2 CTAs
-//             per SM).  With T < 4 they go through a ring of shared-memory
-//             slots three planes ahead of the one being computed, and each
-//             level keeps only the pending plane's partial result and the
-//             last plane's z terms in registers, which makes room for a
-//             third CTA per SM
+//   staging   planes arrive by cp.async (zero fill outside the domain) in
+//             a ring of shared-memory slots three planes ahead of the one
+//             being computed; a plane leaves the ring after its final step
+//             has been compared with it.  Per level the lane keeps the
+//             pending plane's partial result and the last plane's z terms in
+//             registers (3 CTAs of 4 warps per SM)
 //
 // Level s is exact on rows [s, 32 - s) and planes [s, BZ + 2T - s) of the
 // streamed block (errors from the unknown outside creep in one voxel per
-// step; the halo word absorbs x for T < 32), so the interior is exact for all
+// step; the halo word absorbs x for T < 16), so the interior is exact for all
 // s <= T.  At every level the interior is cover-tested (hits are counted with
 // step k_base + s, the distance of those voxels) and the final level is
 // written to the other ping-pong buffer.
@@ -63,27 +61,14 @@ __device__ __forceinline__ void cp_async_wait_upto(int n) {
     }
 }
 
-// All-planes staging, shared memory per warp: the streamed rows (32 B each:
-// 4 interior words, the two halo words, 2 pad words) for NP planes, and the
-// interior uncovered-target words (16 B per row) for BZ planes.
-template <int T, int BZ>
-struct TbSmemAll {
-    static constexpr int NP = BZ + 2 * T;
-    static constexpr int kRowBytes = 32;
-    static constexpr int kURowBytes = 16;
-    static constexpr int kInBytes = NP * 32 * kRowBytes;
-    static constexpr int kWarpBytes = kInBytes + BZ * 32 * kURowBytes;
-    static_assert(kWarpBytes == tb_warp_bytes(T, BZ), "shared layout");
-};
-
-// Ring staging, shared memory of one warp: ring slots of streamed planes (interior words
+// Shared memory of one warp: ring slots of streamed planes (interior words
 // as 16-byte rows, then the two halo words of each row), then the brick's
 // uncovered-target rows.
 template <int T, int BZ>
-struct TbSmemRing {
+struct TbSmem {
     static constexpr int NP = BZ + 2 * T;  // planes streamed per brick
     static constexpr int R = tb_ring_slots(T, BZ);
-    static constexpr int PF = tb_prefetch(T, BZ);  // planes in flight ahead of the one computed
+    static constexpr int PF = kTbPrefetch;  // planes in flight ahead of the one computed
     static constexpr int kInBytes = R * 32 * 16;
     static constexpr int kHaloBytes = R * 32 * 8;
     static constexpr int kUOff = kInBytes + kHaloBytes;
@@ -136,7 +121,7 @@ __device__ __forceinline__ TbRow tb_row(const TbItem& it) {
 // Copies streamed plane r of the brick into its ring slot (one group).
 template <int T, int BZ>
 __device__ __forceinline__ void tb_copy_plane(const TbRow& w, int r, unsigned char* wsm) {
-    using SM = TbSmemRing<T, BZ>;
+    using SM = TbSmem<T, BZ>;
     constexpr int IW = 4;
     const int lane = threadIdx.x & 31;
     const int z = w.z0 - T + r;
@@ -193,61 +178,13 @@ __device__ __forceinline__ bool tb_decode(const SolveParams& p, unsigned long lo
     return true;
 }
 
-// All-planes staging: decodes a queue entry, checks that its job still needs
-// work, and issues every copy of the brick into the warp's shared memory
-// (rows, planes and halo words outside the domain are zero-filled) as one
-// group.  No wait.
-template <int T, int BZ>
-__device__ __forceinline__ void tb_issue_all(const SolveParams& p, unsigned long long e, int g, unsigned char* wsm,
-                                         TbItem& it) {
-    constexpr int IW = 4;
-    constexpr int BYI = 32 - 2 * T;
-    constexpr int NP = BZ + 2 * T;
-    using SM = TbSmemAll<T, BZ>;
-    const int lane = threadIdx.x & 31;
-    if (!tb_decode<T>(p, e, g, it)) return;
-    const Job* Jp = it.Jp;
-    const int Wx = Jp->wx, Hd = Jp->h, Dd = Jp->d;
-    const int wx0 = it.bx * IW, z0 = it.bz * BZ;
-    const int y = it.by * BYI - T + lane;
-    const bool rowv = y >= 0 && y < Hd;
-    const bool inter = rowv && lane >= T && lane < 32 - T;
-    const uint32_t* src = Jp->buf[it.iter & 1];
-    const uint32_t* U = Jp->U;
-    const int pitch = Jp->pitch;
-    const int plane = pitch * Hd;
-    const int rowoff = (rowv ? y : 0) * pitch + wx0;
-    const bool hl_ok = rowv && wx0 > 0;
-    const bool hr_ok = rowv && wx0 + IW < Wx;
-    const uint32_t s_in = (uint32_t)__cvta_generic_to_shared(wsm);
-    const uint32_t s_u = s_in + SM::kInBytes;
-#pragma unroll
-    for (int r = 0; r < NP; ++r) {
-        const int z = z0 - T + r;
-        const bool ok = rowv && z >= 0 && z < Dd;
-        const uint32_t* gp = src + (ok ? z * plane + rowoff : 0);
-        const uint32_t d = s_in + (uint32_t)((r * 32 + lane) * SM::kRowBytes);
-        cp_async16(d, gp, ok ? 16u : 0u);
-        cp_async4(d + 16, (ok && hl_ok) ? gp - 1 : gp, (ok && hl_ok) ? 4u : 0u);
-        cp_async4(d + 20, (ok && hr_ok) ? gp + IW : gp, (ok && hr_ok) ? 4u : 0u);
-    }
-#pragma unroll
-    for (int i = 0; i < BZ; ++i) {
-        const int z = z0 + i;
-        const bool ok = inter && z < Dd;
-        cp_async16(s_u + (uint32_t)((i * 32 + lane) * SM::kURowBytes), U + (ok ? z * plane + rowoff : 0),
-                   ok ? 16u : 0u);
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-}
-
-// Ring staging: decodes a queue entry, checks that its job still needs work, and issues
+// Decodes a queue entry, checks that its job still needs work, and issues
 // the copies of the brick's uncovered-target rows (one group) and of its
 // first planes (one group each).  No wait.
 template <int T, int BZ>
-__device__ __forceinline__ void tb_issue_ring(const SolveParams& p, unsigned long long e, int g, unsigned char* wsm,
+__device__ __forceinline__ void tb_issue(const SolveParams& p, unsigned long long e, int g, unsigned char* wsm,
                                          TbItem& it) {
-    using SM = TbSmemRing<T, BZ>;
+    using SM = TbSmem<T, BZ>;
     const int lane = threadIdx.x & 31;
     if (!tb_decode<T>(p, e, g, it)) return;
     const Job* Jp = it.Jp;
@@ -273,201 +210,16 @@ struct TbOut {
     bool skip;                  // the job had finished: nothing computed, no epilogue
 };
 
-// All-planes staging: waits for the item's copies, runs its T steps (per
-// level a window of M for two planes and Z for three) and writes its state
-// and uncovered-target words back.
-template <int T, int BZ, bool SE18>
-__device__ __forceinline__ void tb_compute_all(const SolveParams& p, const TbItem& it, unsigned char* wsm, TbOut& res) {
-    static_assert(T >= 1 && T <= kTbMaxSteps, "steps per barrier out of range");
-    constexpr int IW = 4;
-    constexpr int NW = IW + 1;  // [combined halo word, 4 interior words]
-    constexpr int BYI = 32 - 2 * T;
-    constexpr int NP = BZ + 2 * T;
-    using SM = TbSmemAll<T, BZ>;
-    const int lane = threadIdx.x & 31;
-    const Job* Jp = it.Jp;
-    res.skip = it.active == 0;
-    if (res.skip) {  // job finished: let the item's copies land (the buffer is reused next) and drop it
-        asm volatile("cp.async.wait_group 0;" ::: "memory");
-        return;
-    }
-    const int Wx = Jp->wx, Hd = Jp->h, Dd = Jp->d;
-    const int wx0 = it.bx * IW, z0 = it.bz * BZ;
-    const int y = it.by * BYI - T + lane;
-    const bool rowv = y >= 0 && y < Hd;
-    const bool inter = rowv && lane >= T && lane < 32 - T;
-    uint32_t* __restrict__ dst = Jp->buf[(it.iter + 1) & 1];
-    uint32_t* __restrict__ U = Jp->U;
-    const int pitch = Jp->pitch;
-    const int plane = pitch * Hd;
-    const int rowoff = (rowv ? y : 0) * pitch + wx0;
-    const int kb = it.kb;
-    uint32_t wm[NW];  // valid bits of each word of this lane's row
-    {
-        uint32_t w6[IW + 2];
-#pragma unroll
-        for (int j = 0; j < IW + 2; ++j) {
-            const int w = wx0 - 1 + j;
-            w6[j] = (rowv && w >= 0 && w < Wx) ? (w == Wx - 1 ? Jp->tailmask : kFull) : 0u;
-        }
-        wm[0] = (w6[0] & 0xffff0000u) | (w6[IW + 1] & 0x0000ffffu);
-#pragma unroll
-        for (int j = 1; j <= IW; ++j) wm[j] = w6[j];
-    }
-    asm volatile("cp.async.wait_group 0;" ::: "memory");  // each lane reads back only its own rows
-
-    auto plane_ok = [&](int r) {  // streamed plane index r -> inside the domain
-        const int z = z0 - T + r;
-        return z >= 0 && z < Dd;
-    };
-    auto in_row = [&](int r) -> const uint32_t* {
-        return reinterpret_cast<const uint32_t*>(wsm + (r * 32 + lane) * SM::kRowBytes);
-    };
-    auto u_row = [&](int i) -> uint32_t* {
-        return reinterpret_cast<uint32_t*>(wsm + SM::kInBytes + (i * 32 + lane) * SM::kURowBytes);
-    };
-    auto load_row = [&](int r, uint32_t (&C)[NW]) {
-        const uint32_t* rp = in_row(r);
-        const uint4 v = *reinterpret_cast<const uint4*>(rp);
-        const uint2 h = *reinterpret_cast<const uint2*>(rp + 4);
-        C[0] = ((h.x & 0xffff0000u) | (h.y & 0x0000ffffu)) & wm[0];
-        C[1] = v.x & wm[1];
-        C[2] = v.y & wm[2];
-        C[3] = v.z & wm[3];
-        C[4] = v.w & wm[4];
-    };
-    // In-plane terms of one level's plane: M = C | sx(C) | sy(C) [| sx(sy(C))],
-    // Z = C [| sx(sy(C))]: what the plane contributes to itself and to the
-    // planes above and below.
-    auto terms = [&](const uint32_t (&C)[NW], uint32_t (&M)[NW], uint32_t (&Z)[NW]) {
-        // rows: lanes 0 and 31 get their own row back from the shuffle,
-        // which is already in M, the same as an empty row outside
-        uint32_t Y[NW];
-#pragma unroll
-        for (int j = 0; j < NW; ++j) Y[j] = __shfl_up_sync(kFull, C[j], 1) | __shfl_down_sync(kFull, C[j], 1);
-        // x: one funnel shift per direction carries the neighbour word's
-        // bit.  The words form a ring [H, I0, I1, I2, I3]: the halo word H
-        // holds the left neighbour word's high half (x0 - 16 .. x0 - 1) in
-        // bits 16-31 and the right neighbour word's low half (x1 + 1 ..
-        // x1 + 16) in bits 0-15, so I3 is H's left and I0 its right
-        // neighbour; the two halves trade bits 15 and 16, 16 voxels from the
-        // interior, which T <= 4 steps never carry back
-#pragma unroll
-        for (int j = 0; j < NW; ++j) {
-            const uint32_t l = C[(j + NW - 1) % NW], r = C[(j + 1) % NW];
-            const uint32_t sx = __funnelshift_l(l, C[j], 1) | __funnelshift_r(C[j], r, 1);
-            if constexpr (!SE18) {
-                M[j] = C[j] | sx | Y[j];
-                Z[j] = C[j];
-            } else {
-                const uint32_t yl = Y[(j + NW - 1) % NW], yr = Y[(j + 1) % NW];
-                const uint32_t sxy = __funnelshift_l(yl, Y[j], 1) | __funnelshift_r(Y[j], yr, 1);
-                M[j] = C[j] | sx | Y[j] | sxy;
-                Z[j] = C[j] | sxy;
-            }
-        }
-    };
-
-    // Register windows of levels 0 .. T-1: M of the last two planes, Z of the
-    // last three.
-    uint32_t Mw[T][2][NW], Zw[T][3][NW];
-    unsigned cnt[T];
-#pragma unroll
-    for (int s = 0; s < T; ++s) cnt[s] = 0;
-    uint32_t d_any = 0, d_xl = 0, d_xh = 0, d_zl = 0, d_zh = 0, u_hits = 0;
-    const bool band_yl = inter && (lane - T) < T;
-    const bool band_yh = inter && (lane - T) >= BYI - T;
-    (void)p;
-
-#pragma unroll
-    for (int q = 0; q < NP; ++q) {
-        {
-            uint32_t C[NW];
-            load_row(q, C);
-            terms(C, Mw[0][q % 2], Zw[0][q % 3]);
-        }
-#pragma unroll
-        for (int s = 1; s <= T; ++s) {
-            const int r = q - s;
-            if (r >= s && r <= NP - 1 - s) {
-                uint32_t out[NW];
-                const bool pv = plane_ok(r);
-#pragma unroll
-                for (int j = 0; j < NW; ++j)
-                    out[j] = pv ? ((Mw[s - 1][r % 2][j] | Zw[s - 1][(r + 2) % 3][j] | Zw[s - 1][(r + 1) % 3][j]) &
-                                   wm[j])
-                                : 0u;
-                if (r >= T && r < T + BZ) {
-                    // cover test of the interior at step kb + s (U rows of
-                    // non-interior lanes and planes are zero)
-                    uint32_t* ur = u_row(r - T);
-                    uint4 u = *reinterpret_cast<const uint4*>(ur);
-                    const uint32_t h0 = out[1] & u.x, h1 = out[2] & u.y, h2 = out[3] & u.z, h3 = out[4] & u.w;
-                    const uint32_t hany = h0 | h1 | h2 | h3;
-                    if (hany) {
-                        cnt[s - 1] += __popc(h0) + __popc(h1) + __popc(h2) + __popc(h3);
-                        u.x &= ~h0;
-                        u.y &= ~h1;
-                        u.z &= ~h2;
-                        u.w &= ~h3;
-                        *reinterpret_cast<uint4*>(ur) = u;
-                        u_hits |= 1u << (r - T);
-                    }
-                }
-                if (s < T) {
-                    terms(out, Mw[s][r % 2], Zw[s][r % 3]);
-                } else {
-                    // final level: store, write back U, record changes
-                    const int z = z0 - T + r;
-                    if (inter && z < Dd) {
-                        const int off = z * plane + rowoff;
-                        *reinterpret_cast<uint4*>(dst + off) = make_uint4(out[1], out[2], out[3], out[4]);
-                        const uint4 c0 = *reinterpret_cast<const uint4*>(in_row(r));
-                        const uint32_t dx0 = out[1] ^ (c0.x & wm[1]), dx3 = out[4] ^ (c0.w & wm[4]);
-                        const uint32_t dall = dx0 | (out[2] ^ (c0.y & wm[2])) | (out[3] ^ (c0.z & wm[3])) | dx3;
-                        // only changes within T voxels of an x face can reach
-                        // the x neighbour's interior during its next T steps
-                        constexpr uint32_t kLoBits = (1u << T) - 1u, kHiBits = ~(0xffffffffu >> T);
-                        if (u_hits & (1u << (r - T)))
-                            *reinterpret_cast<uint4*>(U + off) = *reinterpret_cast<const uint4*>(u_row(r - T));
-                        d_any |= dall;
-                        d_xl |= dx0 & kLoBits;
-                        d_xh |= dx3 & kHiBits;
-                        if (r - T < T) d_zl |= dall;
-                        if (r - T >= BZ - T) d_zh |= dall;
-                    }
-                }
-            }
-        }
-    }
-
-    // per-step hit counts and frontier flags
-#pragma unroll
-    for (int s = 0; s < T; ++s) {
-        unsigned c = cnt[s];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
-        res.cnt[s] = c;
-    }
-    res.any = __any_sync(kFull, d_any != 0);
-    res.fxl = __any_sync(kFull, d_xl != 0);
-    res.fxh = __any_sync(kFull, d_xh != 0);
-    res.fyl = __any_sync(kFull, band_yl && d_any != 0);
-    res.fyh = __any_sync(kFull, band_yh && d_any != 0);
-    res.fzl = __any_sync(kFull, d_zl != 0);
-    res.fzh = __any_sync(kFull, d_zh != 0);
-}
-
-// Ring staging: runs the item's T steps plane by plane, copying planes into
-// the ring PF ahead (per level the pending plane's partial result and the
+// Runs the item's T steps plane by plane, copying planes into the ring PF
+// ahead (per level the pending plane's partial result and the
 // last plane's Z), and writes its state and uncovered-target words back.
 template <int T, int BZ, bool SE18>
-__device__ __forceinline__ void tb_compute_ring(const SolveParams& p, const TbItem& it, unsigned char* wsm, TbOut& res) {
+__device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& it, unsigned char* wsm, TbOut& res) {
     static_assert(T >= 1 && T <= kTbMaxSteps, "steps per barrier out of range");
     constexpr int IW = 4;
     constexpr int NW = IW + 1;  // [combined halo word, 4 interior words]
     constexpr int BYI = 32 - 2 * T;
-    using SM = TbSmemRing<T, BZ>;
+    using SM = TbSmem<T, BZ>;
     constexpr int NP = SM::NP;
     const int lane = threadIdx.x & 31;
     const Job* Jp = it.Jp;
@@ -646,19 +398,6 @@ __device__ __forceinline__ void tb_compute_ring(const SolveParams& p, const TbIt
     res.fzh = __any_sync(kFull, d_zh != 0);
 }
 
-// Staging chosen by T (see tb_all_planes).
-template <int T, int BZ>
-__device__ __forceinline__ void tb_issue(const SolveParams& p, unsigned long long e, int g, unsigned char* wsm,
-                                         TbItem& it) {
-    if constexpr (tb_all_planes(T)) tb_issue_all<T, BZ>(p, e, g, wsm, it);
-    else tb_issue_ring<T, BZ>(p, e, g, wsm, it);
-}
-template <int T, int BZ, bool SE18>
-__device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& it, unsigned char* wsm, TbOut& res) {
-    if constexpr (tb_all_planes(T)) tb_compute_all<T, BZ, SE18>(p, it, wsm, res);
-    else tb_compute_ring<T, BZ, SE18>(p, it, wsm, res);
-}
-
 // Counts, frontier, completion.  The completion atomic's return value is
 // consumed last, so its latency overlaps the frontier atomics.
 template <int T, bool SE18>
@@ -720,7 +459,7 @@ __device__ __forceinline__ void tb_epilogue(const SolveParams& p, const TbItem& 
 }
 
 template <int T, int BZ, bool SE18>
-__global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel(SolveParams p) {
+__global__ void __launch_bounds__(kTbWarps * 32, kTbMinCtas) solve_tb_kernel(SolveParams p) {
     extern __shared__ __align__(16) unsigned char tb_smem[];
     __shared__ int s_flag;
     __shared__ unsigned s_gen, s_cnt;
