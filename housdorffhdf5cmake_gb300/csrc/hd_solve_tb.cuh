@@ -335,9 +335,18 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
                 zp[s - 1][j] = Z[j];
             }
             if (!(r >= s && r <= NP - 1 - s)) break;  // nothing complete at level s yet
-            const bool pv = plane_ok(r);
+            // Clip to the domain.  The 6-neighbour element needs it only at
+            // the last level: the domain is a box and every shortest
+            // 6-neighbour path between two of its voxels stays inside it, so
+            // dilating past its faces for a few levels changes nothing inside
+            // (and the uncovered-target words are zero outside).  The
+            // 18-neighbour element's paths can leave and re-enter the box: it
+            // is clipped at every level, like the reference's border guards.
+            if (SE18 || s == T) {
+                const bool pv = plane_ok(r);
 #pragma unroll
-            for (int j = 0; j < NW; ++j) out[j] = pv ? (out[j] & wm[j]) : 0u;
+                for (int j = 0; j < NW; ++j) out[j] = pv ? (out[j] & wm[j]) : 0u;
+            }
             if (r >= T && r < T + BZ) {
                 // cover test of the interior at step kb + s (U rows of
                 // non-interior lanes and planes are zero)
