@@ -30,7 +30,7 @@ const void* solve_kernel_ptr_se18(int bxw, int bz);
 
 // The temporally blocked kernel (hd_solve_tb.cuh): `steps` dilation steps per
 // grid barrier, bricks of 4 words x (32 - 2 steps) rows x bz planes.
-// Compiled: steps 1, 2 with bz 8, 16; steps 3, 4 with bz 8; both elements.
+// Compiled: steps 1, 2 with bz 8, 16; steps 3, 4, 5 with bz 8; both elements.
 const void* solve_tb_kernel_ptr(int se, int steps, int bz);
 const void* solve_tb_kernel_ptr_se6(int steps, int bz);
 const void* solve_tb_kernel_ptr_se18(int steps, int bz);

@@ -203,7 +203,7 @@ __device__ __forceinline__ void tb_issue(const SolveParams& p, unsigned long lon
 }
 
 // What the epilogue of an item needs from its compute phase.
-constexpr int kTbMaxSteps = 4;
+constexpr int kTbMaxSteps = 5;
 struct TbOut {
     unsigned cnt[kTbMaxSteps];  // newly covered voxels per step of the item
     bool any, fxl, fxh, fyl, fyh, fzl, fzh;
@@ -318,8 +318,9 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
         {
             const uint4 v = in_row(q);
             const uint2 h = halo_row(q);
-            uint32_t C[NW] = {((h.x & 0xffff0000u) | (h.y & 0x0000ffffu)) & wm[0], v.x & wm[1], v.y & wm[2],
-                              v.z & wm[3], v.w & wm[4]};
+            // zero outside the domain already (zero-fill copies, clean tail
+            // bits), so no mask here
+            uint32_t C[NW] = {(h.x & 0xffff0000u) | (h.y & 0x0000ffffu), v.x, v.y, v.z, v.w};
             terms(C, M, Z);
         }
         // (M, Z) hold level s - 1 terms of plane q - s + 1: they complete

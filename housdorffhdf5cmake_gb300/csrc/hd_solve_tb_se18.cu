@@ -15,6 +15,7 @@ const void* solve_tb_kernel_ptr_se18(int steps, int bz) {
     HD_TB_CASE(2, 16)
     HD_TB_CASE(3, 8)
     HD_TB_CASE(4, 8)
+    HD_TB_CASE(5, 8)
     return nullptr;
 }
 

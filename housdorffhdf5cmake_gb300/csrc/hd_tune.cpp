@@ -139,9 +139,9 @@ extern "C" hd_status hd_autotune(hd_context* ctx, const hd_pair_desc* pairs, int
             c.bz = bz;
             cands.push_back(c);
         }
-    for (int steps : {1, 2, 3, 4})
+    for (int steps : {1, 2, 3, 4, 5})
         for (int bz : {8, 16}) {
-            if (steps > 2 && bz != 8) continue;  // compiled: steps 3, 4 with bz 8 only
+            if (steps > 2 && bz != 8) continue;  // compiled: steps 3, 4, 5 with bz 8 only
             Shape c;
             c.kernel = 2;
             c.steps = steps;

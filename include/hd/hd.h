@@ -96,7 +96,7 @@ typedef struct hd_options {
                                     (brick_x_words x 32/brick_x_words rows x brick_z planes),
                                     2 = temporally blocked (steps_per_barrier steps per barrier,
                                     4 words x (32 - 2 steps) rows x brick_z planes) */
-    int32_t steps_per_barrier;   /* kernel 2: 1, 2 (brick_z 8 or 16), 3 or 4 (brick_z 8); 0 = tuned/default */
+    int32_t steps_per_barrier;   /* kernel 2: 1, 2 (brick_z 8 or 16), 3, 4 or 5 (brick_z 8); 0 = tuned/default */
 } hd_options;
 
 /* Device durations of the last call's kernels (record_timings = 1), measured

@@ -118,7 +118,7 @@ def test_brick_shapes_agree(hd, oracle, metric):
                 with hd.Context(0, kernel=1, brick_x_words=bxw, brick_z=bz, ctas_per_sm=cps) as c:
                     g = c.compute(da, db, metric)
                 assert_same(g, o, f"one-step kernel brick {bxw}x{bz} cps {cps}")
-    for steps, bz in ((1, 8), (1, 16), (2, 8), (2, 16), (3, 8), (4, 8)):
+    for steps, bz in ((1, 8), (1, 16), (2, 8), (2, 16), (3, 8), (4, 8), (5, 8)):
         for cps in (0, 1):
             with hd.Context(0, kernel=2, steps_per_barrier=steps, brick_z=bz, ctas_per_sm=cps) as c:
                 g = c.compute(da, db, metric)
@@ -126,7 +126,7 @@ def test_brick_shapes_agree(hd, oracle, metric):
 
 
 @pytest.mark.parametrize("metric", ["se6", "se18"])
-@pytest.mark.parametrize("kernel,steps", [(1, 0), (2, 1), (2, 2), (2, 3), (2, 4)])
+@pytest.mark.parametrize("kernel,steps", [(1, 0), (2, 1), (2, 2), (2, 3), (2, 4), (2, 5)])
 def test_kernels_on_ragged_shapes(hd, oracle, metric, kernel, steps):
     rng = np.random.default_rng(7)
     with hd.Context(0, kernel=kernel, steps_per_barrier=steps) as c:
