@@ -46,6 +46,20 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
     asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
+// Arrival at the grid barrier: release (this CTA's writes before it) and
+// acquire (the writes of the CTAs that arrived before) in one atomic.
+__device__ __forceinline__ unsigned atom_add_acq_rel_u32(unsigned* p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+// Release of the grid barrier: every write before it is visible to a CTA
+// that reads the new value with an acquire load.
+__device__ __forceinline__ void atom_exch_release_u64(unsigned long long* p, unsigned long long v) {
+    unsigned long long old;
+    asm volatile("atom.release.gpu.global.exch.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+    (void)old;
+}
 __device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
     unsigned v;
     asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -72,10 +86,11 @@ __device__ __forceinline__ bool grid_step_barrier(Ctl* ctl, unsigned& gen, int g
     if (threadIdx.x == 0) {
         const unsigned target = gen + 1u;
         unsigned long long rel = 0ull;
-        __threadfence();
-        const unsigned arrived = atomicAdd(&ctl->bar_count, 1u);
+        // the CTA's threads wrote before the __syncthreads above; the
+        // acq_rel arrival publishes those writes (cumulativity) and makes the
+        // earlier arrivals' writes visible to the last CTA
+        const unsigned arrived = atom_add_acq_rel_u32(&ctl->bar_count, 1u);
         if (arrived == gridDim.x - 1u) {
-            __threadfence();
             ctl->bar_count = 0u;
             const int err = ld_relaxed_s32(&ctl->err);
             const int jobs = ld_relaxed_s32(&ctl->jobs_active);
@@ -83,8 +98,7 @@ __device__ __forceinline__ bool grid_step_barrier(Ctl* ctl, unsigned& gen, int g
             const bool cont = err == 0 && jobs > 0 && nq > 0u;
             ctl->qcount[(g + 2) % 3] = 0u;
             rel = ((unsigned long long)target << 32) | (cont ? 0x80000000ull : 0ull) | (nq & 0x7fffffffu);
-            __threadfence();
-            atomicExch(&ctl->release, rel);
+            atom_exch_release_u64(&ctl->release, rel);
         } else {
             // poll hot at first (a barrier normally completes within a few
             // microseconds), then with short sleeps; bounded in time and count
