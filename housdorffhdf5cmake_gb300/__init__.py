@@ -93,6 +93,15 @@ def _check(code: int, ctx_handle, allow_empty=True):
     raise HDError(code, msg)
 
 
+RESULT_BYTES = ctypes.sizeof(N.HdResult)
+
+
+def result_from_bytes(buf) -> dict:
+    """hd_result from its bytes (a CPU uint8 tensor / numpy array / bytes)."""
+    raw = bytes(buf.numpy().tobytes()) if hasattr(buf, "numpy") else bytes(buf)
+    return N.HdResult.from_buffer_copy(raw[:RESULT_BYTES]).as_dict()
+
+
 def _ready(*bufs):
     """Entry points without a stream argument run on the context's own
     stream: finish the work that produced CUDA masks on torch's stream."""
@@ -102,8 +111,12 @@ def _ready(*bufs):
 
 
 def _current_stream_ptr():
+    """torch's current stream as a cudaStream_t for the C ABI.  torch's
+    default stream is the legacy NULL stream, which the C ABI would read as
+    "the context's own stream": pass the cudaStreamLegacy handle (0x1)
+    instead, so the work is ordered with torch's."""
     import torch
-    return torch.cuda.current_stream().cuda_stream
+    return torch.cuda.current_stream().cuda_stream or 0x1
 
 
 class Context:
@@ -197,6 +210,27 @@ class Context:
 
     def compute_device(self, a, b, metric="se6", stream=None) -> dict:
         return self.compute(a, b, metric, stream)
+
+    def compute_async(self, a, b, metric="se6", out=None, stream=None):
+        """Enqueues one pair of CUDA masks on `stream` (default: torch's
+        current stream) and returns at once (hd_compute_u8_device_async).
+        The result lands in `out`, a CUDA uint8 tensor of RESULT_BYTES bytes
+        (allocated if None), once the stream reaches it; decode it with
+        result_from_bytes(out.cpu()).  Calls on one context must stay on one
+        stream."""
+        import torch
+        A, B = _Buf(a), _Buf(b)
+        if not (A.on_device and B.on_device):
+            raise ValueError("compute_async() takes CUDA tensors")
+        if (A.W, A.H, A.D) != (B.W, B.H, B.D):
+            raise ValueError("mask shapes differ")
+        if out is None:
+            out = torch.empty(RESULT_BYTES, dtype=torch.uint8, device=A.obj.device)
+        s = _current_stream_ptr() if stream is None else stream
+        code = N.load().hd_compute_u8_device_async(self._h, A.ptr, B.ptr, A.W, A.H, A.D, metric_code(metric),
+                                                   ctypes.c_void_p(s), ctypes.c_void_p(out.data_ptr()))
+        _check(code, self._h, allow_empty=False)
+        return out
 
     # -- batches --------------------------------------------------------------
     def batch(self, pairs: Sequence, metric="se6") -> list:

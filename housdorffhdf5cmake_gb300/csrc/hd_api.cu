@@ -35,6 +35,8 @@ constexpr long long kMaxWords = (1LL << 31) - 1;
 
 cudaError_t DeviceArena::ensure(size_t n) {
     if (n <= cap) return cudaSuccess;
+    // asynchronous calls may still use the old buffer on some stream
+    if (ptr) cudaDeviceSynchronize();
     release();
     size_t want = std::max(n, cap + cap / 4);
     cudaError_t e = cudaMalloc(&ptr, want);
@@ -339,11 +341,30 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         ctx->stamp_slots = want;
         ctx->g_next = 1;
     }
-    e = ctx->pinned.ensure(pinned_bytes);
+    const bool async = ro.async_out != nullptr;
+    int slot = -1;
+    if (async) {
+        // first asynchronous call: every staging buffer and event at once
+        // (pinned allocations are slow; later calls should not meet one)
+        if (!ctx->async_done[0]) {
+            for (int i = 0; i < hd_context::kAsyncSlots && e == cudaSuccess; ++i) {
+                e = cudaEventCreateWithFlags(&ctx->async_done[i], cudaEventDisableTiming);
+                if (e == cudaSuccess) e = ctx->async_stage[i].ensure(std::max<size_t>(upload_bytes, 1 << 16));
+            }
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "staging buffers");
+        }
+        // a staging buffer whose previous upload has run
+        slot = ctx->async_next;
+        ctx->async_next = (ctx->async_next + 1) % hd_context::kAsyncSlots;
+        e = cudaEventSynchronize(ctx->async_done[slot]);
+        if (e == cudaSuccess) e = ctx->async_stage[slot].ensure(upload_bytes);
+    } else {
+        e = ctx->pinned.ensure(pinned_bytes);
+    }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "pinned staging");
 
     char* dbase = (char*)ctx->arena.ptr;
-    char* hbase = (char*)ctx->pinned.ptr;
+    char* hbase = (char*)(async ? ctx->async_stage[slot].ptr : ctx->pinned.ptr);
     const int g0 = ctx->g_next;
     long long pack_tiles = 0, setup_tiles = 0;
 
@@ -386,6 +407,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
 
     // ---- uploads ----------------------------------------------------------
     e = cudaMemcpyAsync(dbase, hbase, upload_bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && async) e = cudaEventRecord(ctx->async_done[slot], s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "descriptor upload");
     for (int i = 0; i < n; ++i) {
         const size_t nb = (size_t)pairs[i].W * pairs[i].H * pairs[i].D;
@@ -414,7 +436,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     const int grid_pack = (int)std::min<long long>(std::max(ctx->sm_count * 8, 1), pack_tiles);
     const int grid_setup = (int)std::min<long long>(std::max(ctx->sm_count * 8, 1), setup_tiles);
     const PairDesc* ddesc = (const PairDesc*)(dbase + off_descs);
-    const bool timing = ctx->opt.record_timings != 0 && ctx->ev[0] != nullptr;
+    const bool timing = ctx->opt.record_timings != 0 && ctx->ev[0] != nullptr && !async;
     if (timing) cudaEventRecord(ctx->ev[0], s);
     e = hdk::launch_pack(ddesc, n, pack_tiles, grid_pack, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "pack launch");
@@ -459,6 +481,15 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     e = cudaLaunchCooperativeKernel(solve_fn, grid, block, args, (size_t)sh.smem, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "dilation launch");
     if (timing) cudaEventRecord(ctx->ev[3], s);
+    const float pct = (ctx->opt.percentile > 0.f && ctx->opt.percentile <= 1.f) ? ctx->opt.percentile : 0.95f;
+    if (async) {
+        // decode on the device; the step counter moves past any step this
+        // launch can reach (its stamps stay below the next call's steps)
+        e = hdk::launch_finalize(dctl, dstates, ddesc, n, pct, ro.async_out, s);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "result decode launch");
+        ctx->g_next = g0 + sp.max_iters + 2;
+        return HD_OK;
+    }
 
     // ---- read-back ------------------------------------------------------------
     e = cudaMemcpyAsync(hbase, dbase, readback_bytes, cudaMemcpyDeviceToHost, s);
@@ -499,7 +530,6 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         T.steps_per_barrier = sh.steps;
         T.brick_rows = by;
     }
-    const float pct = (ctx->opt.percentile > 0.f && ctx->opt.percentile <= 1.f) ? ctx->opt.percentile : 0.95f;
     hd_status first = HD_OK;
     size_t hoff = 0, toff = 0;
     for (int i = 0; i < n; ++i) {
@@ -627,6 +657,10 @@ hd_status hd_context_destroy(hd_context* ctx) {
         ctx->arena.release();
         ctx->stamps.release();
         ctx->pinned.release();
+        for (int i = 0; i < hd_context::kAsyncSlots; ++i) {
+            ctx->async_stage[i].release();
+            if (ctx->async_done[i]) cudaEventDestroy(ctx->async_done[i]);
+        }
         for (auto& ev : ctx->ev)
             if (ev) cudaEventDestroy(ev);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -690,6 +724,23 @@ hd_status hd_compute_u8_device(hd_context* ctx, const uint8_t* d_a, const uint8_
     RunOpts ro;
     ro.se = se;
     return run_pairs(ctx, &p, 1, stream ? (cudaStream_t)stream : ctx->stream, ro, out);
+}
+
+hd_status hd_compute_u8_device_async(hd_context* ctx, const uint8_t* d_a, const uint8_t* d_b, int32_t W, int32_t H,
+                                     int32_t D, hd_metric metric, void* stream, hd_result* d_out) {
+    if (!ctx || !d_a || !d_b || !d_out) return HD_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    int se = 0;
+    hd_status st = metric_to_se(ctx, metric, &se);
+    if (st == HD_OK) st = check_dims(ctx, W, H, D);
+    if (st != HD_OK) return st;
+    DeviceGuard g(ctx->device);
+    if (!g.ok) return set_error(ctx, HD_ERR_CUDA, "cannot select device %d", ctx->device);
+    PairIn p{d_a, d_b, W, H, D, nullptr, nullptr};
+    RunOpts ro;
+    ro.se = se;
+    ro.async_out = d_out;
+    return run_pairs(ctx, &p, 1, stream ? (cudaStream_t)stream : ctx->stream, ro, nullptr);
 }
 
 hd_status hd_batch_compute(hd_context* ctx, const hd_pair_desc* pairs, int32_t n, hd_result* out) {

@@ -101,6 +101,12 @@ struct hd_context {
     hdh::TuneTable tune;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // record_timings: before pack/setup/solve, after solve
     hd_timings last_timings{};
+    // asynchronous calls: descriptor staging buffers that stay untouched
+    // until their upload has run (an event per buffer)
+    static constexpr int kAsyncSlots = 4;
+    hdh::PinnedArena async_stage[kAsyncSlots];
+    cudaEvent_t async_done[kAsyncSlots] = {nullptr, nullptr, nullptr, nullptr};
+    int async_next = 0;
 };
 
 namespace hdh {
@@ -125,6 +131,7 @@ struct RunOpts {
     uint64_t* bricks = nullptr;
     bool force_shape = false;  // use `shape` as given (autotuner)
     Shape shape;
+    hd_result* async_out = nullptr;  // device memory: enqueue only, results decoded on the device
 };
 
 hd_status set_error(hd_context* ctx, hd_status st, const char* fmt, ...);

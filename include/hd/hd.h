@@ -154,6 +154,18 @@ typedef struct hd_pair_desc {
     int32_t reserved;
 } hd_pair_desc;
 
+/* Asynchronous form of hd_compute_u8_device; no counterpart in the reference
+ * (whose calls block).  Enqueues the whole computation on `stream` (NULL =
+ * the context's stream) and returns: the result is decoded on the device into
+ * *d_out (DEVICE memory, sizeof(hd_result)), valid once the stream reaches
+ * it; errors found on the device are in d_out->status, launch errors are
+ * returned.  Back-to-back calls overlap the host's work with the device's.
+ * The context's workspace is reused by every call, so all calls on one
+ * context (synchronous ones included) must be ordered on one stream.
+ * hd_context_last_timings is not updated. */
+hd_status hd_compute_u8_device_async(hd_context* ctx, const uint8_t* d_a, const uint8_t* d_b, int32_t W,
+                                     int32_t H, int32_t D, hd_metric metric, void* stream, hd_result* d_out);
+
 /* Solves n pairs of independent shapes with one packing launch, one set-up
  * launch and ONE persistent dilation launch over a shared (pair, brick) work
  * queue.  Per-pair results are bit-identical to hd_compute_u8.  out[i].status

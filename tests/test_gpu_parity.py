@@ -298,3 +298,38 @@ def test_context_stream_calls_wait_for_torch_stream(hd, ctx):
     more = [synth.pair_shifted_union(950, (192, 256, 256), "cuda", rmin=8, rmax=60, max_shift=9)]
     with hd.Context(0) as c:
         c.autotune(more, "se6", repeats=1)  # raises if shapes disagree (a half-written mask would)
+
+
+def test_async_entry_matches_blocking_entry(hd, ctx):
+    """hd_compute_u8_device_async: back-to-back calls on one stream (sizes
+    growing and shrinking, both elements, empty masks), results decoded on
+    the device, equal field by field to hd_compute_u8_device."""
+    import ctypes
+    from housdorffhdf5cmake_gb300 import _native as N
+    rng = np.random.default_rng(5)
+    cases = []
+    for i, shape in enumerate([(24, 40, 56), (64, 96, 130), (9, 17, 33), (80, 120, 200), (1, 1, 1)]):
+        a, b = random_pair(rng, shape, p_a=0.02, p_b=0.01)
+        cases.append((a, b, "se6" if i % 2 == 0 else "se18"))
+    z = np.zeros((12, 20, 36), np.uint8)
+    one = z.copy()
+    one[3, 4, 5] = 1
+    cases += [(z, z.copy(), "se6"), (one, z.copy(), "se6"), (one, one.copy(), "se18")]
+    a, b = synth.pair_shifted_union(17, (96, 128, 160), "cpu", rmin=6, rmax=40, max_shift=9)
+    cases.append((a.numpy(), b.numpy(), "se6"))
+    dev = [(cuda(a), cuda(b), m) for a, b, m in cases]
+    with hd.Context(0) as c:
+        outs = [c.compute_async(a, b, m) for a, b, m in dev]  # no synchronisation in between
+        torch.cuda.current_stream().synchronize()
+        got = [hd.result_from_bytes(o.cpu()) for o in outs]
+        want = [c.compute(a, b, m) for a, b, m in dev]
+    for i, (g, w) in enumerate(zip(got, want)):
+        for k in w:
+            if k == "avg_hd" and w[k] != w[k]:
+                assert g[k] != g[k], (i, k)
+            else:
+                assert g[k] == w[k], (i, k, g, w)
+    L = N.load()
+    d = cuda(cases[0][0])
+    assert L.hd_compute_u8_device_async(ctx.handle, d.data_ptr(), d.data_ptr(), 56, 40, 24, 0, None,
+                                        None) == hd.HD_ERR_BAD_ARG
