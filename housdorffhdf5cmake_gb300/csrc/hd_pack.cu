@@ -492,26 +492,39 @@ __global__ void info_init_kernel(const PairDesc* __restrict__ descs, int npairs)
     I->pad[0] = I->pad[1] = 0;
 }
 
-// Robust HD on the device: the stopping rule of hello.cu:1751-1758 (keep
-// dilating while (float)total * p > covered) on a per-step histogram.
-__device__ __forceinline__ int robust_k_device(const unsigned long long* hist, int len, unsigned long long total,
-                                               float p) {
+// Robust HD on the device, one warp: the stopping rule of hello.cu:1751-1758
+// (keep dilating while (float)total * p > covered, covered = voxels with
+// distance 1..k) on a per-step histogram.  covered grows with k, so the
+// first k that stops is found 32 steps at a time by a prefix sum and a
+// ballot (a single thread would wait on one load per step).
+__device__ __forceinline__ int robust_k_warp(const unsigned long long* hist, int len, unsigned long long total,
+                                             float p) {
+    const int lane = threadIdx.x & 31;
     const float tf = (float)total * p;
-    unsigned long long cov = 0;
-    for (int k = 0; k < len; ++k) {
-        if (k > 0) cov += hist[k];
-        if (!(tf > (float)cov)) return k;
+    unsigned long long base = 0;
+    for (int k0 = 0; k0 < len; k0 += 32) {
+        const int k = k0 + lane;
+        unsigned long long c = (k > 0 && k < len) ? hist[k] : 0ull;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long t = __shfl_up_sync(0xffffffffu, c, o);
+            if (lane >= o) c += t;
+        }
+        const bool stop = k < len && !(tf > (float)(base + c));
+        const unsigned m = __ballot_sync(0xffffffffu, stop);
+        if (m) return k0 + __ffs(m) - 1;
+        base += __shfl_sync(0xffffffffu, c, 31);
     }
     return len - 1;
 }
 
-// Decodes each pair's result on the device (one thread per pair), with the
+// Decodes each pair's result on the device (one warp per pair), with the
 // rules of the host decoder: statuses, one-sided distances, exact sums,
 // average (one double division), robust HD.
 __global__ void finalize_kernel(const Ctl* __restrict__ ctl, const JobState* __restrict__ states,
                                 const PairDesc* __restrict__ descs, int npairs, float pct, hd_result* out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= npairs) return;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= npairs) return;  // whole warps leave together
     const PairDesc& P = descs[i];
     const PairInfo I = *P.info;
     const JobState s0 = states[P.job0], s1 = states[P.job0 + 1];
@@ -540,11 +553,11 @@ __global__ void finalize_kernel(const Ctl* __restrict__ ctl, const JobState* __r
         r.hd = max(r.hd_ab, r.hd_ba);
         r.avg_hd = (double)(r.sum_ab + r.sum_ba) / (double)(r.n_a + r.n_b);
         const int kp1 = P.kmax + 1;
-        r.hd_robust = max(robust_k_device(P.hist[1], kp1, r.n_a_not_b, pct),
-                          robust_k_device(P.hist[0], kp1, r.n_b_not_a, pct));
+        r.hd_robust = max(robust_k_warp(P.hist[1], kp1, r.n_a_not_b, pct),
+                          robust_k_warp(P.hist[0], kp1, r.n_b_not_a, pct));
         if (st != HD_OK) r.hd = r.hd_ab = r.hd_ba = r.hd_robust = -1;
     }
-    out[i] = r;
+    if ((threadIdx.x & 31) == 0) out[i] = r;
 }
 
 // Instrumented runs: zero the per-tile stamps and per-step tile counters.
@@ -608,7 +621,7 @@ cudaError_t launch_info_init(const PairDesc* d_descs, int npairs, cudaStream_t s
 cudaError_t launch_finalize(const Ctl* ctl, const JobState* states, const PairDesc* d_descs, int npairs, float pct,
                             hd_result* out, cudaStream_t s) {
     if (npairs <= 0) return cudaSuccess;
-    finalize_kernel<<<(npairs + 127) / 128, 128, 0, s>>>(ctl, states, d_descs, npairs, pct, out);
+    finalize_kernel<<<(npairs + 3) / 4, 128, 0, s>>>(ctl, states, d_descs, npairs, pct, out);  // a warp per pair
     return cudaGetLastError();
 }
 
