@@ -448,7 +448,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
                                  (unsigned long long*)(dbase + off_q[2])};
     if (timing) cudaEventRecord(ctx->ev[1], s);
     e = hdk::launch_setup(ddesc, n, setup_tiles, grid_setup, djobs, dstates, dq[g0 % 3], dctl, g0, bxw, by, bz,
-                          stats ? 1 : 0, s);
+                          sh.kernel == 1 ? 1 : 0, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "setup launch");
     if (ro.map_a || ro.map_b) {
         e = hdk::launch_map_init(ddesc, ro.map_a, ro.map_b,

@@ -12,9 +12,11 @@ namespace hdk {
 // = first tile of pair i, increasing) with `grid` CTAs.  Brick geometry:
 // bxw words x by rows x bz planes (both kernel families).
 cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, int grid, cudaStream_t s);
+// init_second: also initialise each job's second ping-pong buffer (the
+// one-step kernel needs it; the blocked kernel writes it in its first step).
 cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int grid, Job* jobs,
                          JobState* states, unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
-                         int stats, cudaStream_t s);
+                         int init_second, cudaStream_t s);
 // Device-side decode of each pair's result into out[i] (asynchronous entry):
 // the same rules as the host decoder; robust HD at percentile pct.
 cudaError_t launch_finalize(const Ctl* ctl, const JobState* states, const PairDesc* d_descs, int npairs, float pct,

@@ -226,7 +226,7 @@ extern "C" hd_status hd_compute_u8_device_noalloc(const uint8_t* d_a, const uint
                                 (unsigned long long*)(base + L.queue[2])};
     if (e == cudaSuccess)
         e = hdk::launch_setup(desc, 1, stiles, (int)std::min<long long>(cap_ctas, stiles), jobs, states, q[g0 % 3], ctl,
-                              g0, kBxw, 32 / kBxw, kBz, 0, s);
+                              g0, kBxw, 32 / kBxw, kBz, 1, s);  // one-step kernel: both ping-pong buffers
     if (e == cudaSuccess) {
         hdk::SolveParams sp{};
         sp.jobs = jobs;

@@ -361,15 +361,15 @@ __device__ __forceinline__ Domain make_domain(const PairDesc& P, const PairInfo&
 }
 
 __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_pair, Job* jobs, JobState* states,
-                                           unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz);
+                                           unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
+                                           bool init_second);
 
 // 1D grid, block 256: CTAs stride over the tiles of all pairs; tile 0 of a
 // pair also writes its job descriptors.  A pair's tiles cover its full
 // volume's word count, an upper bound of its domain.
 __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__ descs, int npairs, long long ntiles,
                                                     Job* jobs, JobState* states, unsigned long long* queue0,
-                                                    Ctl* ctl, int g0, int bxw, int by, int bz, int stats) {
-    (void)stats;
+                                                    Ctl* ctl, int g0, int bxw, int by, int bz, int init_second) {
     int pi = -1;
     // CTAs stride over the tiles: a pair's domain fills only the first of
     // its tiles, so contiguous runs would leave some CTAs without work
@@ -377,12 +377,13 @@ __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__
         int np = pi < 0 ? pair_of_tile(descs, npairs, tile, true) : pi;
         while (np + 1 < npairs && descs[np + 1].stile0 <= tile) ++np;  // tiles only increase
         pi = np;
-        setup_tile(descs[pi], tile - descs[pi].stile0, jobs, states, queue0, ctl, g0, bxw, by, bz);
+        setup_tile(descs[pi], tile - descs[pi].stile0, jobs, states, queue0, ctl, g0, bxw, by, bz, init_second != 0);
     }
 }
 
 __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_pair, Job* jobs, JobState* states,
-                                           unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz) {
+                                           unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
+                                           bool init_second) {
     const PairInfo I = *P.info;
     const bool empty_a = I.n_a == 0, empty_b = I.n_b == 0;
     const unsigned long long rem[2] = {I.n_b - I.n_ab, I.n_a - I.n_ab};
@@ -440,6 +441,8 @@ __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_
         }
     }
     // Crop copy.  Job 0 dilates A and must cover B; job 1 dilates B and covers A.
+    // buf[1] is written only for the one-step kernel: the blocked kernel's
+    // first iteration processes every brick and writes all of buf[1].
     const long long words = min((long long)m.pitch * m.h * m.d, w_hi);
     const bool act0 = rem[0] > 0, act1 = rem[1] > 0;
     for (long long t = w_lo + tid0; t < words; t += nthr) {
@@ -455,8 +458,16 @@ __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_
             a = __ldg(P.pa + src);
             b = __ldg(P.pb + src);
         }
-        if (act0) { P.jb[0][0][t] = a; P.jb[0][1][t] = a; P.jb[0][2][t] = b & ~a; }
-        if (act1) { P.jb[1][0][t] = b; P.jb[1][1][t] = b; P.jb[1][2][t] = a & ~b; }
+        if (act0) {
+            P.jb[0][0][t] = a;
+            if (init_second) P.jb[0][1][t] = a;
+            P.jb[0][2][t] = b & ~a;
+        }
+        if (act1) {
+            P.jb[1][0][t] = b;
+            if (init_second) P.jb[1][1][t] = b;
+            P.jb[1][2][t] = a & ~b;
+        }
     }
     // First step of each active job: every brick of its domain (one
     // warp-aggregated append per 32 bricks).
@@ -607,8 +618,11 @@ cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, i
 
 cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int grid, Job* jobs,
                          JobState* states, unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
-                         int stats, cudaStream_t s) {
-    setup_kernel<<<grid, 256, 0, s>>>(d_descs, npairs, ntiles, jobs, states, queue0, ctl, g0, bxw, by, bz, stats);
+                         int init_second, cudaStream_t s) {
+    if (grid > ntiles) grid = (int)ntiles;
+    if (grid < 1) grid = 1;
+    setup_kernel<<<grid, 256, 0, s>>>(d_descs, npairs, ntiles, jobs, states, queue0, ctl, g0, bxw, by, bz,
+                                      init_second);
     return cudaGetLastError();
 }
 

@@ -297,7 +297,7 @@ void tick(hd_server* s) {
             e = hdk::launch_setup(s->d_descs, (int)admitted.size(), stiles, (int)std::min<long long>(cap_ctas, stiles),
                                   s->d_jobs, s->d_states,
                                   s->d_queue[s->g_next % 3], s->d_ctl, s->g_next, s->shape.bxw, s->shape.by,
-                                  s->shape.bz, 0, st);
+                                  s->shape.bz, s->shape.kernel == 1 ? 1 : 0, st);
         // no wait here: the host masks' copies read the requests' own
         // buffers (alive until completion), the descriptors' staging area is
         // rewritten only after the end-of-tick synchronisation, and the
