@@ -67,7 +67,7 @@ constexpr long long kTileWords = 1024;
 // uncovered-target rows (BZ planes x 32 rows x 16 B).  3 CTAs of kTbWarps
 // warps fit on an SM.
 constexpr int kTbWarps = 4;
-constexpr int kTbPrefetch = 3;
+constexpr int kTbPrefetch = 2;
 constexpr int kTbMinCtas = 3;
 __host__ __device__ constexpr int tb_ring_slots(int T, int BZ) {
     return T + 1 + kTbPrefetch >= BZ + 2 * T ? BZ + 2 * T : T + 1 + kTbPrefetch;

@@ -14,7 +14,7 @@
 //             planes; rows come from the neighbouring lanes by shuffle, x
 //             carries from the neighbouring words of the row
 //   staging   planes arrive by cp.async (zero fill outside the domain) in
-//             a ring of shared-memory slots three planes ahead of the one
+//             a ring of shared-memory slots two planes ahead of the one
 //             being computed; a plane leaves the ring after its final step
 //             has been compared with it.  Per level the lane keeps the
 //             pending plane's partial result and the last plane's z terms in
