@@ -128,12 +128,14 @@ class Context:
     ctas_per_sm (0 = occupancy maximum), max_iterations (0 = W+H+D),
     barrier_timeout_ns (0 = 10 s), percentile (robust HD, default 0.95),
     zero_copy (host masks read in place when the device can), tuning_table
-    (JSON path of the autotuner's table).
+    (JSON path of the autotuner's table), label (0 = nonzero voxels are
+    foreground; 1..255 = voxels equal to label, the reference's
+    numberToLookFor).
     """
 
     def __init__(self, device: int = 0, *, brick_x_words=0, brick_z=0, ctas_per_sm=0, max_iterations=0,
                  barrier_timeout_ns=0, percentile=0.95, zero_copy=True, tuning_table=None,
-                 record_timings=False, kernel=0, steps_per_barrier=0):
+                 record_timings=False, kernel=0, steps_per_barrier=0, label=0):
         L = N.load()
         opt = N.HdOptions()
         L.hd_options_init(ctypes.byref(opt))
@@ -149,6 +151,7 @@ class Context:
         opt.record_timings = 1 if record_timings else 0
         opt.kernel = int(kernel)
         opt.steps_per_barrier = int(steps_per_barrier)
+        opt.label = int(label)
         h = ctypes.c_void_p()
         code = L.hd_context_create(int(device), ctypes.byref(opt), ctypes.byref(h))
         if code != HD_OK:

@@ -71,6 +71,7 @@ class HdOptions(ctypes.Structure):
         ("record_timings", ctypes.c_int32),
         ("kernel", ctypes.c_int32),
         ("steps_per_barrier", ctypes.c_int32),
+        ("label", ctypes.c_int32),
     ]
 
 

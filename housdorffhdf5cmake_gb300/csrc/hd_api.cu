@@ -438,7 +438,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     const PairDesc* ddesc = (const PairDesc*)(dbase + off_descs);
     const bool timing = ctx->opt.record_timings != 0 && ctx->ev[0] != nullptr && !async;
     if (timing) cudaEventRecord(ctx->ev[0], s);
-    e = hdk::launch_pack(ddesc, n, pack_tiles, grid_pack, s);
+    e = hdk::launch_pack(ddesc, n, pack_tiles, grid_pack, ctx->opt.label, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "pack launch");
     Ctl* dctl = (Ctl*)(dbase + off_ctl);
     Job* djobs = (Job*)(dbase + off_jobs);
@@ -452,7 +452,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     if (e != cudaSuccess) return cuda_fail(ctx, e, "setup launch");
     if (ro.map_a || ro.map_b) {
         e = hdk::launch_map_init(ddesc, ro.map_a, ro.map_b,
-                                 (long long)pairs[0].W * pairs[0].H * pairs[0].D, s);
+                                 (long long)pairs[0].W * pairs[0].H * pairs[0].D, ctx->opt.label, s);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "map init launch");
     }
 
@@ -607,6 +607,7 @@ const char* hd_version(void) { return "hd_gb300 1.0 sm_103a"; }
 hd_status hd_context_create(int device, const hd_options* opt, hd_context** out) {
     if (!out) return HD_ERR_BAD_ARG;
     *out = nullptr;
+    if (opt && (opt->label < 0 || opt->label > 255)) return HD_ERR_BAD_ARG;
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess) {

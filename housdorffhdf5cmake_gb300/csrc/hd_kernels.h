@@ -11,7 +11,8 @@ namespace hdk {
 // Packing and set-up run over `ntiles` tiles of kTileWords words (descs[i].tile0
 // = first tile of pair i, increasing) with `grid` CTAs.  Brick geometry:
 // bxw words x by rows x bz planes (both kernel families).
-cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, int grid, cudaStream_t s);
+// label: 0 = every nonzero byte is foreground, 1..255 = bytes equal to label.
+cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, int grid, int label, cudaStream_t s);
 // init_second: also initialise each job's second ping-pong buffer (the
 // one-step kernel needs it; the blocked kernel writes it in its first step).
 cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int grid, Job* jobs,
@@ -24,7 +25,7 @@ cudaError_t launch_finalize(const Ctl* ctl, const JobState* states, const PairDe
 // Start values of descs[i].info (counts 0, empty bounding box), i < npairs.
 cudaError_t launch_info_init(const PairDesc* d_descs, int npairs, cudaStream_t s);
 cudaError_t launch_zero_i32(int32_t* p, long long n, cudaStream_t s);
-cudaError_t launch_map_init(const PairDesc* d_descs, int32_t* map_a, int32_t* map_b, long long n,
+cudaError_t launch_map_init(const PairDesc* d_descs, int32_t* map_a, int32_t* map_b, long long n, int label,
                             cudaStream_t s);
 
 // The persistent dilation kernel for one (element, brick width, brick depth).

@@ -218,7 +218,8 @@ extern "C" hd_status hd_compute_u8_device_noalloc(const uint8_t* d_a, const uint
     const long long ptiles = hdk::tiles_of(hdk::pack_words(W, H, D));
     const long long stiles = hdk::tiles_of(hdk::domain_cap_words(W, H, D));
     const int cap_ctas = std::max(slot->sm_count * 8, 1);
-    if (e == cudaSuccess) e = hdk::launch_pack(desc, 1, ptiles, (int)std::min<long long>(cap_ctas, ptiles), s);
+    if (e == cudaSuccess)  // nonzero bytes are foreground
+        e = hdk::launch_pack(desc, 1, ptiles, (int)std::min<long long>(cap_ctas, ptiles), 0, s);
     hdk::Job* jobs = (hdk::Job*)(base + L.jobs);
     hdk::JobState* states = (hdk::JobState*)(base + L.states);
     hdk::Ctl* ctl = (hdk::Ctl*)(base + L.ctl);

@@ -21,21 +21,28 @@
 
 namespace hdk {
 
-// Nonzero bytes of a 32-bit word as flags at bits 28..31 (byte i -> bit
-// 28 + i).  The normalised word has bits only at 7, 15, 23, 31; times
-// 2^0 + 2^7 + 2^14 + 2^21 its partial products land on distinct bits (7, 14,
-// 15, 21, 22, 23 below 28, the flags at 28..31), so nothing carries.
-__device__ __forceinline__ uint32_t nz4_top(uint32_t w) {
-    const uint32_t t = (((w & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | w) & 0x80808080u;
+// Foreground bytes of a 32-bit word as flags at bits 28..31 (byte i -> bit
+// 28 + i).  Foreground = nonzero, or (kLabel) equal to the label, whose
+// byte `pat` repeats four times: the XOR turns those bytes into zeros and
+// the zero-byte flags are the complement of the nonzero ones.  The
+// normalised word has bits only at 7, 15, 23, 31; times 2^0 + 2^7 + 2^14 +
+// 2^21 its partial products land on distinct bits (7, 14, 15, 21, 22, 23
+// below 28, the flags at 28..31), so nothing carries.
+template <bool kLabel>
+__device__ __forceinline__ uint32_t fg4_top(uint32_t w, uint32_t pat) {
+    if constexpr (kLabel) w ^= pat;
+    uint32_t t = (((w & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | w) & 0x80808080u;
+    if constexpr (kLabel) t ^= 0x80808080u;
     return t * 0x00204081u;
 }
 
-// Nonzero bytes of 16 bytes -> 16 bits (byte i -> bit i).  The partial
+// Foreground bytes of 16 bytes -> 16 bits (byte i -> bit i).  The partial
 // products below bit 24 vanish in the two larger shifts and are masked off in
 // the two smaller ones.
-__device__ __forceinline__ uint32_t nz16(uint4 v) {
-    return (nz4_top(v.x) >> 28) | (nz4_top(v.y) >> 24) | ((nz4_top(v.z) >> 20) & 0xF00u) |
-           ((nz4_top(v.w) >> 16) & 0xF000u);
+template <bool kLabel>
+__device__ __forceinline__ uint32_t fg16(uint4 v, uint32_t pat) {
+    return (fg4_top<kLabel>(v.x, pat) >> 28) | (fg4_top<kLabel>(v.y, pat) >> 24) |
+           ((fg4_top<kLabel>(v.z, pat) >> 20) & 0xF00u) | ((fg4_top<kLabel>(v.w, pat) >> 16) & 0xF000u);
 }
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
@@ -134,16 +141,18 @@ __device__ __forceinline__ void flush_acc(const PairDesc& P, const PackAcc& acc)
     }
 }
 
-// Nonzero bytes among the 16 at p that lie inside [lo, hi), as 16 bits (a
-// mask's first and last 16-byte chunks may stick out of it).  The byte loads
+// Foreground bytes (nonzero, or equal to a nonzero label) among the 16 at p
+// that lie inside [lo, hi), as 16 bits (a mask's first and last 16-byte
+// chunks may stick out of it).  The byte loads
 // are predicated, not branched over, so all sixteen are in flight together.
-__device__ __noinline__ uint32_t chunk_bits_edge(const uint8_t* p, const uint8_t* lo, const uint8_t* hi) {
+__device__ __noinline__ uint32_t chunk_bits_edge(const uint8_t* p, const uint8_t* lo, const uint8_t* hi, int label) {
     uint32_t bits = 0;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
         const bool in = p + i >= lo && p + i < hi;
         const uint8_t v = in ? __ldg(p + i) : (uint8_t)0;
-        bits |= (v != 0 ? 1u : 0u) << i;
+        const bool fg = label ? (in && v == (uint8_t)label) : (v != 0);
+        bits |= (fg ? 1u : 0u) << i;
     }
     return bits;
 }
@@ -194,9 +203,9 @@ __device__ __forceinline__ PackWalk make_walk(const PairDesc& P) {
 // kEdge = false: every word of the tile is in the pair and every chunk it
 // touches lies inside the masks (see pack_kernel); kEdge = true: both are
 // checked word by word.
-template <bool kEdge>
+template <bool kEdge, bool kLabel>
 __device__ __forceinline__ void pack_tile(const PairDesc& P, const PackWalk& k, long long tile_in_pair,
-                                          PackAcc& acc) {
+                                          PackAcc& acc, int label, uint32_t pat) {
     const int lane = threadIdx.x & 31;
     const unsigned t0 = (unsigned)(tile_in_pair * kTileWords) + (threadIdx.x >> 5) * (32u * kPackGroups) + lane;
     unsigned r = t0 / k.wxf, w = t0 - r * k.wxf;
@@ -249,12 +258,12 @@ __device__ __forceinline__ void pack_tile(const PairDesc& P, const PackWalk& k, 
             if (kEdge) {
                 const uint8_t* q = (const uint8_t*)((uintptr_t)(k.src[m] + off) & ~(uintptr_t)15);
                 if (t < k.total && !(q >= k.src[m] && q + 48 <= k.end[m])) {
-                    lo[i][m] = chunk_bits_edge(q, k.src[m], k.end[m]) |
-                               (chunk_bits_edge(q + 16, k.src[m], k.end[m]) << 16);
+                    lo[i][m] = chunk_bits_edge(q, k.src[m], k.end[m], label) |
+                               (chunk_bits_edge(q + 16, k.src[m], k.end[m], label) << 16);
                     continue;
                 }
             }
-            lo[i][m] = nz16(c[i][m][0]) | (nz16(c[i][m][1]) << 16);
+            lo[i][m] = fg16<kLabel>(c[i][m][0], pat) | (fg16<kLabel>(c[i][m][1], pat) << 16);
         }
     }
 #pragma unroll
@@ -277,10 +286,10 @@ __device__ __forceinline__ void pack_tile(const PairDesc& P, const PackWalk& k, 
             if (own3 && sh + nbits > 32) {  // rare: the warp's last word, the pair's last word
                 if (kEdge) {
                     const uint8_t* q = (const uint8_t*)((uintptr_t)(k.src[m] + off) & ~(uintptr_t)15);
-                    hi = (q >= k.src[m] && q + 48 <= k.end[m]) ? nz16(c3[m])  // loaded above
-                                                                : chunk_bits_edge(q + 32, k.src[m], k.end[m]);
+                    hi = (q >= k.src[m] && q + 48 <= k.end[m]) ? fg16<kLabel>(c3[m], pat)  // loaded above
+                                                                : chunk_bits_edge(q + 32, k.src[m], k.end[m], label);
                 } else {
-                    hi = nz16(c3[m]);
+                    hi = fg16<kLabel>(c3[m], pat);
                 }
             }
             out[m] = __funnelshift_r(lo[i][m], hi, sh) & (last ? k.tail : 0xffffffffu);
@@ -299,8 +308,10 @@ __device__ __forceinline__ void pack_tile(const PairDesc& P, const PackWalk& k, 
 // tile or reaches within 48 words of the pair's end: every other word then
 // starts at byte >= kTileWords (each word holds >= 1 byte) and ends >= 48
 // bytes before the mask's end, so its three chunks lie inside the mask.
+template <bool kLabel>
 __global__ void __launch_bounds__(kPackThreads, 2) pack_kernel(const PairDesc* __restrict__ descs, int npairs,
-                                                               long long ntiles) {
+                                                               long long ntiles, int label) {
+    const uint32_t pat = (uint32_t)label * 0x01010101u;
     PackAcc acc;
     PackWalk walk;
     int pi = -1;
@@ -320,9 +331,9 @@ __global__ void __launch_bounds__(kPackThreads, 2) pack_kernel(const PairDesc* _
         }
         const long long tp = tile - descs[pi].tile0;
         if (tp >= 1 && (tp + 1) * kTileWords + 48 <= (long long)walk.total)
-            pack_tile<false>(descs[pi], walk, tp, acc);
+            pack_tile<false, kLabel>(descs[pi], walk, tp, acc, label, pat);
         else
-            pack_tile<true>(descs[pi], walk, tp, acc);
+            pack_tile<true, kLabel>(descs[pi], walk, tp, acc, label, pat);
     }
     if (pi >= 0) flush_acc(descs[pi], acc);
 }
@@ -580,12 +591,12 @@ __global__ void zero_i32_kernel(int32_t* p, long long n) {
 
 // Per-voxel maps: -1 outside the mask, 0 on the overlap, and (filled later by
 // the dilation) the distance on voxels of one mask outside the other.
-__global__ void map_init_kernel(const PairDesc* __restrict__ descs, int32_t* map_a, int32_t* map_b) {
+__global__ void map_init_kernel(const PairDesc* __restrict__ descs, int32_t* map_a, int32_t* map_b, int label) {
     const PairDesc& P = descs[0];
     const long long n = (long long)P.W * P.H * P.D;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
          t += (long long)gridDim.x * blockDim.x) {
-        const bool a = P.a[t] != 0, b = P.b[t] != 0;
+        const bool a = label ? P.a[t] == label : P.a[t] != 0, b = label ? P.b[t] == label : P.b[t] != 0;
         map_a[t] = a ? (b ? 0 : -2) : -1;  // -2: to be filled by the dilation
         map_b[t] = b ? (a ? 0 : -2) : -1;
     }
@@ -596,23 +607,27 @@ __global__ void map_init_kernel(const PairDesc* __restrict__ descs, int32_t* map
 // ---- launch wrappers (called from the host orchestration) -----------------
 namespace hdk {
 
-cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, int grid, cudaStream_t s) {
-    // one wave of resident CTAs (per device, from the occupancy calculator)
-    static int resident[64] = {0};
+cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, int grid, int label, cudaStream_t s) {
+    // one wave of resident CTAs (per device and variant, from the occupancy calculator)
+    static int resident[2][64] = {{0}};
+    const int v = label ? 1 : 0;
+    const void* fn = label ? reinterpret_cast<const void*>(&pack_kernel<true>)
+                           : reinterpret_cast<const void*>(&pack_kernel<false>);
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (dev < 64 && resident[dev] == 0) {
+    if (dev < 64 && resident[v][dev] == 0) {
         int per_sm = 0, sms = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pack_kernel, kPackThreads, 0);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPackThreads, 0);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return e;
-        resident[dev] = std::max(1, per_sm) * std::max(1, sms);
+        resident[v][dev] = std::max(1, per_sm) * std::max(1, sms);
     }
-    if (dev < 64) grid = resident[dev];
+    if (dev < 64) grid = resident[v][dev];
     if (grid > ntiles) grid = (int)ntiles;
     if (grid < 1) grid = 1;
-    pack_kernel<<<grid, kPackThreads, 0, s>>>(d_descs, npairs, ntiles);
+    if (label) pack_kernel<true><<<grid, kPackThreads, 0, s>>>(d_descs, npairs, ntiles, label);
+    else pack_kernel<false><<<grid, kPackThreads, 0, s>>>(d_descs, npairs, ntiles, 0);
     return cudaGetLastError();
 }
 
@@ -647,11 +662,11 @@ cudaError_t launch_zero_i32(int32_t* p, long long n, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_map_init(const PairDesc* d_descs, int32_t* map_a, int32_t* map_b, long long n,
+cudaError_t launch_map_init(const PairDesc* d_descs, int32_t* map_a, int32_t* map_b, long long n, int label,
                             cudaStream_t s) {
     long long blocks = (n + 255) / 256;
     if (blocks > 8192) blocks = 8192;
-    map_init_kernel<<<(int)blocks, 256, 0, s>>>(d_descs, map_a, map_b);
+    map_init_kernel<<<(int)blocks, 256, 0, s>>>(d_descs, map_a, map_b, label);
     return cudaGetLastError();
 }
 

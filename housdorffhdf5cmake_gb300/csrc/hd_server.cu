@@ -292,7 +292,8 @@ void tick(hd_server* s) {
         if (e == cudaSuccess) e = hdk::launch_info_init(s->d_descs, (int)descs.size(), st);
         const int cap_ctas = std::max(s->ctx->sm_count * 8, 1);
         if (e == cudaSuccess)
-            e = hdk::launch_pack(s->d_descs, (int)admitted.size(), ptiles, (int)std::min<long long>(cap_ctas, ptiles), st);
+            e = hdk::launch_pack(s->d_descs, (int)admitted.size(), ptiles, (int)std::min<long long>(cap_ctas, ptiles),
+                                 s->ctx->opt.label, st);
         if (e == cudaSuccess)
             e = hdk::launch_setup(s->d_descs, (int)admitted.size(), stiles, (int)std::min<long long>(cap_ctas, stiles),
                                   s->d_jobs, s->d_states,

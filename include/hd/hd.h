@@ -97,6 +97,9 @@ typedef struct hd_options {
                                     2 = temporally blocked (steps_per_barrier steps per barrier,
                                     4 words x (32 - 2 steps) rows x brick_z planes) */
     int32_t steps_per_barrier;   /* kernel 2: 1, 2 (brick_z 8 or 16), 3, 4 or 5 (brick_z 8); 0 = tuned/default */
+    int32_t label;               /* foreground voxels: 0 = every nonzero byte (default); 1..255 = the bytes
+                                    equal to `label` (the prototype's numberToLookFor, hello.cu:133,615),
+                                    so one uint8 label volume serves every structure it holds */
 } hd_options;
 
 /* Device durations of the last call's kernels (record_timings = 1), measured

@@ -11,7 +11,7 @@ int main(void) {
     F(hd_result, sum_ab); F(hd_result, avg_hd); F(hd_result, status); F(hd_result, hd_robust);
     printf("hd_options %zu\n", sizeof(hd_options));
     F(hd_options, barrier_timeout_ns); F(hd_options, percentile); F(hd_options, tuning_table);
-    F(hd_options, record_timings); F(hd_options, kernel); F(hd_options, steps_per_barrier);
+    F(hd_options, record_timings); F(hd_options, kernel); F(hd_options, steps_per_barrier); F(hd_options, label);
     printf("hd_timings %zu\n", sizeof(hd_timings));
     F(hd_timings, iterations); F(hd_timings, brick_z); F(hd_timings, brick_rows);
     printf("hd_pair_desc %zu\n", sizeof(hd_pair_desc));

@@ -333,3 +333,32 @@ def test_async_entry_matches_blocking_entry(hd, ctx):
     d = cuda(cases[0][0])
     assert L.hd_compute_u8_device_async(ctx.handle, d.data_ptr(), d.data_ptr(), 56, 40, 24, 0, None,
                                         None) == hd.HD_ERR_BAD_ARG
+
+
+def test_label_selection(hd, ctx, oracle):
+    """label option (the reference's numberToLookFor): a voxel is foreground
+    iff its byte equals the label; results equal the binary path on the
+    thresholded masks, for device, host and batched inputs and the maps."""
+    a, b = synth.pair_shifted_union(23, (40, 72, 100), "cpu", rmin=5, rmax=25, max_shift=7)
+    a, b = a.numpy(), b.numpy()
+    rng = np.random.default_rng(13)
+    va = np.where(a != 0, 3, np.where(rng.random(a.shape) < 0.05, 1, 0)).astype(np.uint8)
+    vb = np.where(b != 0, 3, np.where(rng.random(b.shape) < 0.05, 7, 0)).astype(np.uint8)
+    keys = ("hd", "hd_ab", "hd_ba", "sum_ab", "sum_ba", "n_a", "n_b", "n_a_not_b", "n_b_not_a", "status", "hd_robust")
+    for label in (3, 1):
+        ta, tb = (va == label).astype(np.uint8), (vb == label).astype(np.uint8)
+        for metric in ("se6", "se18"):
+            want = ctx.compute(cuda(ta), cuda(tb), metric)
+            o = oracle.forbench(ta, tb, metric)
+            assert want["hd"] == o["hd"] and want["sum_ab"] == o["sum_ab"]
+            with hd.Context(0, label=label) as c:
+                for got in (c.compute(cuda(va), cuda(vb), metric), c.compute(va, vb, metric),
+                            c.batch([(cuda(va), cuda(vb))], metric)[0]):
+                    for k in keys:
+                        assert got[k] == want[k], (label, metric, k, got, want)
+                if metric == "se6":
+                    _, ma, mb = c.distance_map(cuda(va), cuda(vb), metric)
+                    _, wa, wb = ctx.distance_map(cuda(ta), cuda(tb), metric)
+                    assert torch.equal(ma, wa) and torch.equal(mb, wb)
+    with pytest.raises(hd.HDError):
+        hd.Context(0, label=256)
