@@ -13,9 +13,10 @@ available; the masks are seeded synthetic stand-ins with the stated shapes.
          around the K steps; two distinct pairs alternate so every step reads
          masks that are not in L2 (2 x 134 MB > 126 MB L2).  The blocking
          device entry (hd_compute_u8_device) is reported beside it
-  e2e    pairs/s through hd_compute_u8 with pinned HOST masks: the device
-         reads the masks over the host link inside the call, results come back
-         to the host
+  e2e    pairs/s with pinned HOST masks through hd_compute_u8_async: each
+         pair's masks are copied over the host link (DMA) while the previous
+         pair computes, and each result is read back to the host; the
+         blocking hd_compute_u8 (one call per pair) is reported beside it
 Extra keys: Gvoxel-iter/s, the roofline of the dominant kernel, the serial
 CPU baseline (the oracle's restatement of the reference loop, 1 core), the
 ragged 256-pair batch (one persistent launch) against the same pairs one call
@@ -197,36 +198,53 @@ def bench_ours(args):
     value = ws * 1000.0 / step_ms
 
     # ---- end to end through the host API (pinned host masks) ----------------
+    # Pipelined: hd_compute_u8_async copies each pair's pinned host masks by
+    # DMA on the context's copy stream while the previous pair computes; each
+    # step's 64-byte result is read back to pinned host memory on the stream.
     hpairs = [(x.cpu().pin_memory(), y.cpu().pin_memory()) for x, y in pairs]
-    for w in range(max(1, args.warmup)):
-        assert ctx.compute(*hpairs[w % 2], "se6") == refs[w % 2]
-    e2e_t = []
+    rbytes = hd.RESULT_BYTES
+    e_outs = torch.empty((args.steps, rbytes), dtype=torch.uint8, device=dev)
+    h_outs = torch.empty((args.steps, rbytes), dtype=torch.uint8).pin_memory()
+    for w in range(max(args.warmup, 6)):
+        ctx.compute_async(*hpairs[w % 2], "se6", out=e_outs[w % args.steps])
+    torch.cuda.synchronize()
     if dist:
         dist.barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        ctx.compute_async(*hpairs[k % 2], "se6", out=e_outs[k])
+        h_outs[k].copy_(e_outs[k], non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+    for k in range(args.steps):
+        assert hd.result_from_bytes(h_outs[k]) == refs[k % 2], f"e2e step {k}: result differs"
+    # blocking: one hd_compute_u8 call per pair (the pack kernel reads the
+    # pinned masks in place over the host link), and the same with explicit
+    # host-to-device copies instead of in-place reads
+    for w in range(max(1, args.warmup)):
+        assert ctx.compute(*hpairs[w % 2], "se6") == refs[w % 2]
+    blk_t = []
     for k in range(args.steps):
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        t1 = time.perf_counter()
         r = ctx.compute(*hpairs[k % 2], "se6")
-        e2e_t.append((time.perf_counter() - t0) * 1000.0)
+        blk_t.append((time.perf_counter() - t1) * 1000.0)
         assert r == refs[k % 2]
-    e2e_ms = sum(e2e_t) / len(e2e_t)
-    # the same with explicit host-to-device copies instead of in-place reads
+    blocking_e2e_ms = sum(blk_t) / len(blk_t)
     staged_ms = None
     with hd.Context(local, zero_copy=False) as sctx:
         assert sctx.compute(*hpairs[0], "se6") == refs[0]
         st_t = []
         for k in range(args.steps):
             torch.cuda.synchronize()
-            t0 = time.perf_counter()
+            t1 = time.perf_counter()
             sctx.compute(*hpairs[k % 2], "se6")
-            st_t.append((time.perf_counter() - t0) * 1000.0)
+            st_t.append((time.perf_counter() - t1) * 1000.0)
         staged_ms = sum(st_t) / len(st_t)
     if dist:
         t = torch.tensor([e2e_ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
-    kmax = W_ + H_ + D_
-    d2h = 768 + 2 * 8 * (kmax + 1)
 
     # ---- roofline of the dominant kernel -------------------------------------
     # algorithmic bytes of the dilation (mean of the two pairs, like the times)
@@ -292,8 +310,11 @@ def bench_ours(args):
         "barrier_iterations": [phases[0]["iterations"], phases[1]["iterations"]],
         "gvoxel_iter_per_s": round(gvox, 2),
         "e2e": {"value": round(ws * 1000.0 / e2e_ms, 3), "unit": "pairs/s", "ms_per_step": round(e2e_ms, 4),
-                "h2d_bytes_per_step": 2 * N, "d2h_bytes_per_step": d2h,
-                "path": "hd_compute_u8, pinned host masks read by the packing kernel over the host link",
+                "h2d_bytes_per_step": 2 * N, "d2h_bytes_per_step": rbytes,
+                "path": "hd_compute_u8_async: pinned host masks copied by DMA while the previous pair computes, "
+                        "result read back to host each step; wall clock over the K steps",
+                "blocking_ms_per_step": round(blocking_e2e_ms, 4),
+                "blocking_path": "hd_compute_u8, one call per pair, masks read in place over the host link",
                 "staged_copy_ms_per_step": round(staged_ms, 4)},
         "gpu_launches": 4 * args.steps,
         "blocking_call": {"path": "hd_compute_u8_device (returns the result to the host each call)",

@@ -215,23 +215,28 @@ class Context:
         return self.compute(a, b, metric, stream)
 
     def compute_async(self, a, b, metric="se6", out=None, stream=None):
-        """Enqueues one pair of CUDA masks on `stream` (default: torch's
-        current stream) and returns at once (hd_compute_u8_device_async).
-        The result lands in `out`, a CUDA uint8 tensor of RESULT_BYTES bytes
-        (allocated if None), once the stream reaches it; decode it with
-        result_from_bytes(out.cpu()).  Calls on one context must stay on one
-        stream."""
+        """Enqueues one pair on `stream` (default: torch's current stream) and
+        returns at once: CUDA masks through hd_compute_u8_device_async, host
+        masks (numpy / CPU tensors; pinned for a truly asynchronous copy)
+        through hd_compute_u8_async, whose copy overlaps the previous pair's
+        kernels.  The result lands in `out`, a CUDA uint8 tensor of
+        RESULT_BYTES bytes (allocated if None), once the stream reaches it;
+        decode it with result_from_bytes(out.cpu()).  Host masks must stay
+        unchanged until then.  Calls on one context must stay on one stream."""
         import torch
         A, B = _Buf(a), _Buf(b)
-        if not (A.on_device and B.on_device):
-            raise ValueError("compute_async() takes CUDA tensors")
         if (A.W, A.H, A.D) != (B.W, B.H, B.D):
             raise ValueError("mask shapes differ")
+        if A.on_device != B.on_device:
+            raise ValueError("both masks must be on the host or both on the device")
         if out is None:
-            out = torch.empty(RESULT_BYTES, dtype=torch.uint8, device=A.obj.device)
+            dev = A.obj.device if A.on_device else torch.device("cuda", self.device)
+            out = torch.empty(RESULT_BYTES, dtype=torch.uint8, device=dev)
         s = _current_stream_ptr() if stream is None else stream
-        code = N.load().hd_compute_u8_device_async(self._h, A.ptr, B.ptr, A.W, A.H, A.D, metric_code(metric),
-                                                   ctypes.c_void_p(s), ctypes.c_void_p(out.data_ptr()))
+        L = N.load()
+        fn = L.hd_compute_u8_device_async if A.on_device else L.hd_compute_u8_async
+        code = fn(self._h, A.ptr, B.ptr, A.W, A.H, A.D, metric_code(metric), ctypes.c_void_p(s),
+                  ctypes.c_void_p(out.data_ptr()))
         _check(code, self._h, allow_empty=False)
         return out
 

@@ -318,8 +318,8 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         for (int j = 0; j < 2; ++j)
             for (int b = 0; b < 3; ++b) q.off_jb[j][b] = take(4ULL * q.dom_words);
         const size_t nb = (size_t)pairs[i].W * pairs[i].H * pairs[i].D;
-        q.off_in_a = pairs[i].host_a ? take(nb) : 0;
-        q.off_in_b = pairs[i].host_b ? take(nb) : 0;
+        q.off_in_a = (pairs[i].host_a && !ro.async_out) ? take(nb) : 0;
+        q.off_in_b = (pairs[i].host_b && !ro.async_out) ? take(nb) : 0;
         if (stats) {
             for (int j = 0; j < 2; ++j) {
                 q.off_tstamp[j] = take(sizeof(int32_t) * q.tiles);
@@ -368,6 +368,38 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     const int g0 = ctx->g_next;
     long long pack_tiles = 0, setup_tiles = 0;
 
+    // ---- asynchronous calls with host masks: copy on the copy stream ------
+    const uint8_t* staged[2] = {nullptr, nullptr};
+    int mb = -1;
+    if (async && n == 1 && (pairs[0].host_a || pairs[0].host_b)) {
+        if (!ctx->copy_stream) {
+            e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+            for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+                e = cudaEventCreateWithFlags(&ctx->mask_ready[i], cudaEventDisableTiming);
+                if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->mask_free[i], cudaEventDisableTiming);
+            }
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "copy stream");
+        }
+        mb = ctx->mask_next;
+        ctx->mask_next ^= 1;
+        const size_t nb = (size_t)pairs[0].W * pairs[0].H * pairs[0].D;
+        e = ctx->mask_stage[mb].ensure(2 * align_up(nb));
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "mask staging");
+        uint8_t* sa = (uint8_t*)ctx->mask_stage[mb].ptr;
+        uint8_t* sb = sa + align_up(nb);
+        // the packing that read this buffer two calls ago must be done
+        e = cudaStreamWaitEvent(ctx->copy_stream, ctx->mask_free[mb], 0);
+        if (e == cudaSuccess && pairs[0].host_a)
+            e = cudaMemcpyAsync(sa, pairs[0].host_a, nb, cudaMemcpyHostToDevice, ctx->copy_stream);
+        if (e == cudaSuccess && pairs[0].host_b)
+            e = cudaMemcpyAsync(sb, pairs[0].host_b, nb, cudaMemcpyHostToDevice, ctx->copy_stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->mask_ready[mb], ctx->copy_stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ctx->mask_ready[mb], 0);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "mask copy");
+        staged[0] = pairs[0].host_a ? sa : nullptr;
+        staged[1] = pairs[0].host_b ? sb : nullptr;
+    }
+
     // ---- host-side descriptors ------------------------------------------
     std::memset(hbase, 0, upload_bytes);
     PairInfo* hinfo = (PairInfo*)(hbase + off_infos);
@@ -379,8 +411,8 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         I.bb[0] = I.bb[2] = I.bb[4] = 0x7fffffff;
         I.bb[1] = I.bb[3] = I.bb[5] = -1;
         PairDesc& Dd = hdesc[i];
-        Dd.a = P.host_a ? (const uint8_t*)(dbase + q.off_in_a) : P.a;
-        Dd.b = P.host_b ? (const uint8_t*)(dbase + q.off_in_b) : P.b;
+        Dd.a = P.host_a ? (staged[0] ? staged[0] : (const uint8_t*)(dbase + q.off_in_a)) : P.a;
+        Dd.b = P.host_b ? (staged[1] ? staged[1] : (const uint8_t*)(dbase + q.off_in_b)) : P.b;
         Dd.pa = (uint32_t*)(dbase + q.off_pa);
         Dd.pb = (uint32_t*)(dbase + q.off_pb);
         for (int j = 0; j < 2; ++j) {
@@ -409,7 +441,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     e = cudaMemcpyAsync(dbase, hbase, upload_bytes, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && async) e = cudaEventRecord(ctx->async_done[slot], s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "descriptor upload");
-    for (int i = 0; i < n; ++i) {
+    for (int i = 0; i < n && mb < 0; ++i) {
         const size_t nb = (size_t)pairs[i].W * pairs[i].H * pairs[i].D;
         if (pairs[i].host_a) {
             e = cudaMemcpyAsync(dbase + plan[i].off_in_a, pairs[i].host_a, nb, cudaMemcpyHostToDevice, s);
@@ -439,6 +471,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     const bool timing = ctx->opt.record_timings != 0 && ctx->ev[0] != nullptr && !async;
     if (timing) cudaEventRecord(ctx->ev[0], s);
     e = hdk::launch_pack(ddesc, n, pack_tiles, grid_pack, ctx->opt.label, s);
+    if (e == cudaSuccess && mb >= 0) e = cudaEventRecord(ctx->mask_free[mb], s);  // staging buffer read
     if (e != cudaSuccess) return cuda_fail(ctx, e, "pack launch");
     Ctl* dctl = (Ctl*)(dbase + off_ctl);
     Job* djobs = (Job*)(dbase + off_jobs);
@@ -662,6 +695,13 @@ hd_status hd_context_destroy(hd_context* ctx) {
             ctx->async_stage[i].release();
             if (ctx->async_done[i]) cudaEventDestroy(ctx->async_done[i]);
         }
+        if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+        for (int i = 0; i < 2; ++i) {
+            ctx->mask_stage[i].release();
+            if (ctx->mask_ready[i]) cudaEventDestroy(ctx->mask_ready[i]);
+            if (ctx->mask_free[i]) cudaEventDestroy(ctx->mask_free[i]);
+        }
+        if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
         for (auto& ev : ctx->ev)
             if (ev) cudaEventDestroy(ev);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -738,6 +778,23 @@ hd_status hd_compute_u8_device_async(hd_context* ctx, const uint8_t* d_a, const 
     DeviceGuard g(ctx->device);
     if (!g.ok) return set_error(ctx, HD_ERR_CUDA, "cannot select device %d", ctx->device);
     PairIn p{d_a, d_b, W, H, D, nullptr, nullptr};
+    RunOpts ro;
+    ro.se = se;
+    ro.async_out = d_out;
+    return run_pairs(ctx, &p, 1, stream ? (cudaStream_t)stream : ctx->stream, ro, nullptr);
+}
+
+hd_status hd_compute_u8_async(hd_context* ctx, const uint8_t* a, const uint8_t* b, int32_t W, int32_t H, int32_t D,
+                              hd_metric metric, void* stream, hd_result* d_out) {
+    if (!ctx || !a || !b || !d_out) return HD_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    int se = 0;
+    hd_status st = metric_to_se(ctx, metric, &se);
+    if (st == HD_OK) st = check_dims(ctx, W, H, D);
+    if (st != HD_OK) return st;
+    DeviceGuard g(ctx->device);
+    if (!g.ok) return set_error(ctx, HD_ERR_CUDA, "cannot select device %d", ctx->device);
+    PairIn p{nullptr, nullptr, W, H, D, a, b};
     RunOpts ro;
     ro.se = se;
     ro.async_out = d_out;

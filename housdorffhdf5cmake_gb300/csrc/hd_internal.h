@@ -107,6 +107,13 @@ struct hd_context {
     hdh::PinnedArena async_stage[kAsyncSlots];
     cudaEvent_t async_done[kAsyncSlots] = {nullptr, nullptr, nullptr, nullptr};
     int async_next = 0;
+    // asynchronous calls with host masks: two device buffers the masks are
+    // copied into on a copy stream, so a pair's copy overlaps the previous
+    // pair's kernels (ready: copy done; free: the packing that read it done)
+    cudaStream_t copy_stream = nullptr;
+    hdh::DeviceArena mask_stage[2];
+    cudaEvent_t mask_ready[2] = {nullptr, nullptr}, mask_free[2] = {nullptr, nullptr};
+    int mask_next = 0;
 };
 
 namespace hdh {

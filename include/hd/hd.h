@@ -169,6 +169,16 @@ typedef struct hd_pair_desc {
 hd_status hd_compute_u8_device_async(hd_context* ctx, const uint8_t* d_a, const uint8_t* d_b, int32_t W,
                                      int32_t H, int32_t D, hd_metric metric, void* stream, hd_result* d_out);
 
+/* Asynchronous form of hd_compute_u8 (HOST masks); no counterpart in the
+ * reference.  The masks are copied by DMA on the context's copy stream into
+ * one of two device staging buffers, so the copy of one pair overlaps the
+ * kernels of the previous one; the rest is as hd_compute_u8_device_async
+ * (result decoded into *d_out, device memory, when `stream` reaches it).
+ * The host masks must stay unchanged until then; pinned memory makes the
+ * copy asynchronous (pageable memory is copied before the call returns). */
+hd_status hd_compute_u8_async(hd_context* ctx, const uint8_t* a, const uint8_t* b, int32_t W, int32_t H,
+                              int32_t D, hd_metric metric, void* stream, hd_result* d_out);
+
 /* Solves n pairs of independent shapes with one packing launch, one set-up
  * launch and ONE persistent dilation launch over a shared (pair, brick) work
  * queue.  Per-pair results are bit-identical to hd_compute_u8.  out[i].status

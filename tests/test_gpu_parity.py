@@ -362,3 +362,34 @@ def test_label_selection(hd, ctx, oracle):
                     assert torch.equal(ma, wa) and torch.equal(mb, wb)
     with pytest.raises(hd.HDError):
         hd.Context(0, label=256)
+
+
+def test_async_host_entry_pipelines_copies(hd, ctx):
+    """hd_compute_u8_async: host masks (pinned and pageable) copied on the copy
+    stream into alternating staging buffers while earlier pairs compute;
+    every result equals the blocking host entry's."""
+    rng = np.random.default_rng(21)
+    cases = []
+    for i, shape in enumerate([(30, 50, 70), (64, 96, 130), (12, 20, 36), (80, 120, 200), (64, 96, 130)]):
+        a, b = random_pair(rng, shape, p_a=0.02, p_b=0.01)
+        cases.append((a, b, "se6" if i % 2 == 0 else "se18"))
+    one = np.zeros((12, 20, 36), np.uint8)
+    one[3, 4, 5] = 1
+    cases.append((one, np.zeros_like(one), "se6"))
+    host = []
+    for i, (a, b, m) in enumerate(cases):
+        if i % 2 == 0:
+            host.append((torch.from_numpy(a).pin_memory(), torch.from_numpy(b).pin_memory(), m))
+        else:
+            host.append((a, b, m))
+    with hd.Context(0) as c:
+        outs = [c.compute_async(a, b, m) for a, b, m in host]
+        torch.cuda.current_stream().synchronize()
+        got = [hd.result_from_bytes(o.cpu()) for o in outs]
+        want = [c.compute(a, b, m) for a, b, m in cases]
+    for i, (g, w) in enumerate(zip(got, want)):
+        for k in w:
+            if k == "avg_hd" and w[k] != w[k]:
+                assert g[k] != g[k], (i, k)
+            else:
+                assert g[k] == w[k], (i, k, g, w)
