@@ -425,28 +425,44 @@ def bench_serving(ctx, args):
         subq = queue.Queue()
         with hd.Server(ctx, hbm_budget_bytes=120 << 30) as srv:
             def collect():
+                # blocks in hd_server_wait on the oldest outstanding request
+                # (woken by its completion), then picks up any later ones
+                # that finished meanwhile
                 live = []
                 seen = 0
+
+                def done(r, i, t_sub):
+                    lat[i] = time.perf_counter() - t_sub
+                    w = want[i % pool_n]
+                    if any(r[k] != w[k] for k in keys):
+                        exact[0] = False
+
                 while seen < n_req:
                     try:
+                        if not live:
+                            live.append(subq.get(timeout=5.0))
                         while True:
                             live.append(subq.get_nowait())
                     except queue.Empty:
                         pass
+                    if not live:
+                        continue
                     still = []
                     for (t, i, t_sub) in live:
                         r = srv.poll(t)
                         if r is None:
                             still.append((t, i, t_sub))
-                            continue
-                        lat[i] = time.perf_counter() - t_sub
-                        seen += 1
-                        w = want[i % pool_n]
-                        if any(r[k] != w[k] for k in keys):
-                            exact[0] = False
+                        else:
+                            done(r, i, t_sub)
+                            seen += 1
                     live = still
-                    if not live:
-                        time.sleep(20e-6)
+                    if live:  # nothing else finished: sleep in the server until the oldest does (<= 1 ms)
+                        t, i, t_sub = live[0]
+                        r = srv.wait(t, 1)
+                        if r is not None:
+                            done(r, i, t_sub)
+                            seen += 1
+                            live = live[1:]
             th = threading.Thread(target=collect)
             th.start()
             t0 = time.perf_counter()
