@@ -137,10 +137,11 @@ __device__ __forceinline__ void tb_copy_plane(const TbRow& w, int r, unsigned ch
     cp_async_commit();
 }
 
-// Decodes a queue entry and decides whether the item runs (its job still
-// needs work, the entry is not left over from a slot's previous pair, the
-// step cap is not passed).  The job state and every job field the item reads
-// are loaded in one batch, so their latencies overlap.
+// Decodes a queue entry and decides whether the item runs (the entry is not
+// left over from a slot's previous pair, the step cap is not passed).  The
+// job's active flag and every job field the item reads are loaded in one
+// batch, so their latencies overlap; the flag is checked when the item is
+// computed.
 template <int T>
 __device__ __forceinline__ bool tb_decode(const SolveParams& p, unsigned long long e, int g, TbItem& it) {
     const int lane = threadIdx.x & 31;
@@ -178,9 +179,9 @@ __device__ __forceinline__ bool tb_decode(const SolveParams& p, unsigned long lo
     return true;
 }
 
-// Decodes a queue entry, checks that its job still needs work, and issues
-// the copies of the brick's uncovered-target rows (one group) and of its
-// first planes (one group each).  No wait.
+// Decodes a queue entry (tb_decode) and issues the copies of the brick's
+// uncovered-target rows (one group) and of its first planes (one group
+// each).  No wait.
 template <int T, int BZ>
 __device__ __forceinline__ void tb_issue(const SolveParams& p, unsigned long long e, int g, unsigned char* wsm,
                                          TbItem& it) {
@@ -211,11 +212,12 @@ struct TbOut {
 };
 
 // Runs the item's T steps plane by plane, copying planes into the ring PF
-// ahead (per level the pending plane's partial result and the
-// last plane's Z), and writes its state and uncovered-target words back.
+// ahead (per level the pending plane's partial result and the last plane's Z
+// stay in registers), and writes its state and uncovered-target words back.
+// An item whose job finished since it was issued is dropped here.
 template <int T, int BZ, bool SE18>
 __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& it, unsigned char* wsm, TbOut& res) {
-    static_assert(T >= 1 && T <= kTbMaxSteps, "steps per barrier out of range");
+    static_assert(T >= 1 && T <= kTbMaxSteps && kTbMaxSteps < 16, "steps per barrier out of range");
     constexpr int IW = 4;
     constexpr int NW = IW + 1;  // [combined halo word, 4 interior words]
     constexpr int BYI = 32 - 2 * T;
@@ -275,7 +277,7 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
         // bits 16-31 and the right neighbour word's low half (x1 + 1 ..
         // x1 + 16) in bits 0-15, so I3 is H's left and I0 its right
         // neighbour; the two halves trade bits 15 and 16, 16 voxels from the
-        // interior, which T <= 4 steps never carry back
+        // interior, which T <= kTbMaxSteps (< 16) steps never carry back
 #pragma unroll
         for (int j = 0; j < NW; ++j) {
             const uint32_t l = C[(j + NW - 1) % NW], r = C[(j + 1) % NW];
