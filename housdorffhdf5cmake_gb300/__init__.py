@@ -61,6 +61,41 @@ def _dims(x):
     return W, H, D
 
 
+def _fast_cuda(x):
+    """(pointer, W, H, D) of a contiguous 3-D uint8 CUDA tensor, else None."""
+    if type(x).__module__.startswith("torch") and x.is_cuda and x.dim() == 3 and x.is_contiguous():
+        import torch
+        if x.dtype == torch.uint8:
+            D, H, W = x.shape
+            return (x.data_ptr(), int(W), int(H), int(D))
+    return None
+
+
+_PAIR_DESC_DTYPE = np.dtype({
+    "names": [f for f, _ in N.HdPairDesc._fields_],
+    "formats": [np.uintp, np.uintp, np.int32, np.int32, np.int32, np.int32, np.int32, np.int32],
+    "offsets": [getattr(N.HdPairDesc, f).offset for f, _ in N.HdPairDesc._fields_],
+    "itemsize": ctypes.sizeof(N.HdPairDesc),
+})
+
+
+_RESULT_FIELDS = [f for f, _ in N.HdResult._fields_]
+_RESULT_DTYPE = np.dtype({
+    "names": _RESULT_FIELDS,
+    "formats": [{ctypes.c_int32: np.int32, ctypes.c_uint64: np.uint64, ctypes.c_double: np.float64}[t]
+                for _, t in N.HdResult._fields_],
+    "offsets": [getattr(N.HdResult, f).offset for f in _RESULT_FIELDS],
+    "itemsize": ctypes.sizeof(N.HdResult),
+})
+
+
+def _result_dicts(res, n):
+    """hd_result array -> list of dicts, column-wise through numpy."""
+    arr = np.frombuffer(res, dtype=_RESULT_DTYPE, count=n)
+    cols = [arr[f].tolist() for f in _RESULT_FIELDS]
+    return [dict(zip(_RESULT_FIELDS, vals)) for vals in zip(*cols)]
+
+
 class _Buf:
     """Pointer to a contiguous uint8 view of a mask (keeps the owner alive)."""
 
@@ -242,26 +277,41 @@ class Context:
 
     # -- batches --------------------------------------------------------------
     def batch(self, pairs: Sequence, metric="se6") -> list:
-        """One hd_batch_compute over [(a, b), ...] (host or CUDA masks)."""
+        """One hd_batch_compute over [(a, b), ...] (host or CUDA masks).
+        The descriptor array is filled column-wise through numpy (per-field
+        ctypes writes would cost more than the device work of small pairs)."""
         n = len(pairs)
         if n == 0:
             return []
-        bufs = []
-        descs = (N.HdPairDesc * n)()
+        keep, rows = [], []
+        any_dev = False
         for i, (a, b) in enumerate(pairs):
+            fa, fb = _fast_cuda(a), _fast_cuda(b)
+            if fa is not None and fb is not None:
+                if fa[1:] != fb[1:]:
+                    raise ValueError(f"pair {i}: shapes differ")
+                rows.append((fa[0], fb[0]) + fa[1:] + (1,))
+                any_dev = True
+                continue
             A, B = _Buf(a), _Buf(b)
             if (A.W, A.H, A.D) != (B.W, B.H, B.D) or A.on_device != B.on_device:
                 raise ValueError(f"pair {i}: shapes or devices differ")
-            bufs.append((A, B))
-            descs[i].a, descs[i].b = A.ptr, B.ptr
-            descs[i].W, descs[i].H, descs[i].D = A.W, A.H, A.D
-            descs[i].metric = metric_code(metric)
-            descs[i].on_device = 1 if A.on_device else 0
+            keep.append((A, B))
+            any_dev = any_dev or A.on_device
+            rows.append((A.ptr, B.ptr, A.W, A.H, A.D, 1 if A.on_device else 0))
+        descs = np.zeros(n, dtype=_PAIR_DESC_DTYPE)
+        cols = list(zip(*rows))
+        descs["a"], descs["b"] = cols[0], cols[1]
+        descs["W"], descs["H"], descs["D"] = cols[2], cols[3], cols[4]
+        descs["metric"] = metric_code(metric)
+        descs["on_device"] = cols[5]
         res = (N.HdResult * n)()
-        _ready(*[x for ab in bufs for x in ab])
-        code = N.load().hd_batch_compute(self._h, descs, n, res)
+        if any_dev:
+            import torch
+            torch.cuda.current_stream().synchronize()  # this call runs on the context's stream
+        code = N.load().hd_batch_compute(self._h, descs.ctypes.data_as(ctypes.POINTER(N.HdPairDesc)), n, res)
         _check(code, self._h)
-        return [res[i].as_dict() for i in range(n)]
+        return _result_dicts(res, n)
 
     # -- instrumentation --------------------------------------------------------
     def profile(self, a, b, metric="se6"):
