@@ -407,7 +407,8 @@ __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_
     const int kmax = P.kmax;
     // histograms are zeroed for every pair
     if (first)
-        for (long long t = tid0; t < 2LL * (kmax + 1); t += nthr) P.hist[t / (kmax + 1)][t % (kmax + 1)] = 0ull;
+        for (int j = 0; j < 2; ++j)
+            for (int t = (int)tid0; t <= kmax; t += (int)nthr) P.hist[j][t] = 0ull;
     if (empty_a || empty_b) {
         if (first && tid0 == 0) {
             for (int j = 0; j < 2; ++j) {
@@ -485,7 +486,8 @@ __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_
     // the bricks are split evenly over the pair's tiles
     const int lane = threadIdx.x & 31;
     const long long gwarp = tid0 >> 5, nwarps = nthr >> 5;
-    const long long b_per = (nbricks + ntiles_pair - 1) / ntiles_pair;
+    // < 2^31 bricks and tiles per pair: 32-bit division
+    const long long b_per = (long long)(((unsigned)nbricks + (unsigned)ntiles_pair - 1u) / (unsigned)ntiles_pair);
     const long long b_lo = tile_in_pair * b_per, b_hi = min(nbricks, b_lo + b_per);
     for (int j = 0; j < 2; ++j) {
         if (!(j == 0 ? act0 : act1)) continue;
