@@ -344,6 +344,11 @@ def bench_batched(ctx, args):
     specs = synth.batch_ragged_specs(77, n=256)
     pairs = [synth.pair_from_spec(s, "cuda") for s in specs]
     voxels = sum(s.shape[0] * s.shape[1] * s.shape[2] for s in specs)
+    # the autotuner times every compiled brick shape / steps per barrier /
+    # grid size on these pairs (checking they agree) and keeps the fastest
+    # for this workload class; the timed batches below use its choice
+    report = ctx.autotune(pairs, "se6", repeats=1)
+    tuned = [ln for ln in report.splitlines() if ln.startswith("best")]
     batch = ctx.batch(pairs, "se6")
     plain = [ctx.compute(a, b, "se6") for a, b in pairs]
     # every result field except `iterations` (the shared loop's length in a batch)
@@ -379,6 +384,10 @@ def bench_batched(ctx, args):
                              "solve": round(bt["solve_ms"], 3), "barrier_iterations": bt["iterations"]},
         "pack_gbs_batched": round((2 * voxels + 2 * voxels / 8) / (bt["pack_ms"] * 1e-3) / 1e9, 1),
         "bit_exact_vs_plain": bool(exact),
+        "autotuned": tuned[0] if tuned else None,
+        "shape": {"kernel": bt["kernel"], "steps_per_barrier": bt["steps_per_barrier"],
+                  "brick_words_rows_planes": [bt["brick_x_words"], bt["brick_rows"], bt["brick_z"]],
+                  "grid_ctas": bt["grid_ctas"]},
     }
 
 
@@ -530,6 +539,14 @@ def bench_worst_case(ctx, dev):
     dom_bricks_1 = -(-wx // 4) * -(-(hi[1] - lo[1] + 1) // 8) * -(-(hi[0] - lo[0] + 1) // 8)
     iters = max(1, res["hd_ab"]) + max(1, res["hd_ba"])  # profile() runs the one-step kernel
     N = 512 ** 3
+    # per dilation step: 32^3 tiles (of the 16^3 = 4096 of the volume) that
+    # gained voxels, both directions; their algorithmic bytes over the solve
+    n_tiles = (512 // 32) ** 3
+    steps = max(res["hd_ab"], res["hd_ba"])
+    per_step = [(int(tab[k]) if k <= res["hd_ab"] else 0) + (int(tba[k]) if k <= res["hd_ba"] else 0)
+                for k in range(1, steps + 1)]
+    frac = [x / (2 * n_tiles) for x in per_step]
+    alg = 3 * 4096 * sum(per_step)
     return {
         "workload": "512^3, 8 balls r 3-6 vs 8 balls >= 200 voxels away, 6-neighbour element",
         "hd": r["hd"], "barrier_iterations": tim["iterations"], "steps_per_barrier": tim["steps_per_barrier"],
@@ -537,6 +554,9 @@ def bench_worst_case(ctx, dev):
         "pairs_per_s": round(1000.0 / t, 3),
         "gvoxel_iter_per_s": round(r["hd"] * 2 * N / (t * 1e-3) / 1e9, 2),
         "active_brick_fraction_mean": round(bricks / (dom_bricks_1 * iters), 4),
+        "active_tile_fraction_per_step": {"every_25th": [round(f, 4) for f in frac[::25]],
+                                          "mean": round(statistics.mean(frac), 4), "max": round(max(frac), 4)},
+        "solve_algorithmic_gbs": round(alg / (tim["solve_ms"] * 1e-3) / 1e9, 1),
         "solve_ms": round(tim["solve_ms"], 3), "pack_ms": round(tim["pack_ms"], 3),
     }
 
