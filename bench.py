@@ -372,6 +372,11 @@ def bench_batched(ctx, args):
     t_batch = timed(lambda: ctx.batch(pairs, "se6"), reps)
     bt = ctx.last_timings()
     t_plain = timed(lambda: [ctx.compute(a, b, "se6") for a, b in pairs], reps)
+    # device time alone (CUDA events around the kernels of each call)
+    dev_plain = 0.0
+    for a, b in pairs:
+        ctx.compute(a, b, "se6")
+        dev_plain += ctx.last_timings()["total_ms"]
     gvox = sum(max(0, r["hd"]) * 2 * (s.shape[0] * s.shape[1] * s.shape[2]) for r, s in zip(batch, specs))
     return {
         "workload": "256 ragged pairs, axes uniform in {64..384}, 5% edge pairs (empty / identical)",
@@ -379,6 +384,8 @@ def bench_batched(ctx, args):
         "batched_pairs_per_s": round(256 * 1000.0 / t_batch, 2), "batched_ms": round(t_batch, 3),
         "plain_pairs_per_s": round(256 * 1000.0 / t_plain, 2), "plain_ms": round(t_plain, 3),
         "speedup_batched_vs_plain": round(t_plain / t_batch, 2),
+        "device_ms": {"batched": round(bt["total_ms"], 3), "plain_sum": round(dev_plain, 3),
+                      "speedup": round(dev_plain / bt["total_ms"], 2)},
         "gvoxel_iter_per_s_batched": round(gvox / (t_batch * 1e-3) / 1e9, 2),
         "batched_phase_ms": {"pack": round(bt["pack_ms"], 3), "setup": round(bt["setup_ms"], 3),
                              "solve": round(bt["solve_ms"], 3), "barrier_iterations": bt["iterations"]},
