@@ -61,14 +61,24 @@ def _dims(x):
     return W, H, D
 
 
+_torch = None
+
+
 def _fast_cuda(x):
-    """(pointer, W, H, D) of a contiguous 3-D uint8 CUDA tensor, else None."""
-    if type(x).__module__.startswith("torch") and x.is_cuda and x.dim() == 3 and x.is_contiguous():
+    """(pointer, W, H, D) of a contiguous 3-D uint8 CUDA tensor, else None
+    (a handful of attribute reads: batches touch hundreds of tensors)."""
+    global _torch
+    if _torch is None:
+        if not type(x).__module__.startswith("torch"):
+            return None
         import torch
-        if x.dtype == torch.uint8:
-            D, H, W = x.shape
-            return (x.data_ptr(), int(W), int(H), int(D))
-    return None
+        _torch = torch
+    if type(x) is not _torch.Tensor or x.dtype is not _torch.uint8 or not x.is_cuda or not x.is_contiguous():
+        return None
+    sh = x.shape
+    if len(sh) != 3:
+        return None
+    return (x.data_ptr(), sh[2], sh[1], sh[0])
 
 
 _PAIR_DESC_DTYPE = np.dtype({
@@ -286,11 +296,12 @@ class Context:
         keep, rows = [], []
         any_dev = False
         for i, (a, b) in enumerate(pairs):
-            fa, fb = _fast_cuda(a), _fast_cuda(b)
-            if fa is not None and fb is not None:
+            fa = _fast_cuda(a)
+            fb = _fast_cuda(b) if fa is not None else None
+            if fb is not None:
                 if fa[1:] != fb[1:]:
                     raise ValueError(f"pair {i}: shapes differ")
-                rows.append((fa[0], fb[0]) + fa[1:] + (1,))
+                rows.append((fa[0], fb[0], fa[1], fa[2], fa[3], 1))
                 any_dev = True
                 continue
             A, B = _Buf(a), _Buf(b)
