@@ -13,9 +13,11 @@
 //               pad words zero.  The domain is the bounding box of A u B with
 //               x widened to whole words (6-neighbour element) or the whole
 //               volume (18-neighbour element).
-//   bricks      the unit of work: BXW words (x) x (32 / BXW) rows (y) x BZ
-//               planes (z), one warp per brick, lane (lx, ly) owns one word
-//               column and walks z.
+//   bricks      the unit of work of the persistent loop, one warp per brick:
+//               one-step kernel (hd_solve.cuh): BXW words (x) x (32 / BXW)
+//               rows (y) x BZ planes (z), lane (lx, ly) owns one word column
+//               and walks z; blocked kernel (hd_solve_tb.cuh): 4 words x
+//               (32 - 2T) rows x BZ planes, lane = one row.
 #pragma once
 #include <stdint.h>
 
