@@ -290,7 +290,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         PairPlan& q = plan[i];
         const PairIn& P = pairs[i];
         q.wxf = (P.W + 31) / 32;
-        q.full_words = (long long)q.wxf * P.H * P.D;
+        q.full_words = (long long)hdk::packed_pitch(P.W) * P.H * P.D;
         const long long pitch = (q.wxf + 3) / 4 * 4;
         q.dom_words = pitch * P.H * P.D;
         q.bricks = (long long)((q.wxf + bxw - 1) / bxw) * ((P.H + by - 1) / by) * ((P.D + bz - 1) / bz);
@@ -367,6 +367,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     char* hbase = (char*)(async ? ctx->async_stage[slot].ptr : ctx->pinned.ptr);
     const int g0 = ctx->g_next;
     long long pack_tiles = 0, setup_tiles = 0;
+    const int setup_mode = sh.kernel == 1 ? hdk::kSetupOneStep : (n == 1 ? hdk::kSetupBlocked : hdk::kSetupBlockedInPlace);
 
     // ---- asynchronous calls with host masks: copy on the copy stream ------
     const uint8_t* staged[2] = {nullptr, nullptr};
@@ -434,7 +435,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         Dd.tile0 = pack_tiles;
         Dd.stile0 = setup_tiles;
         pack_tiles += hdk::tiles_of(hdk::pack_words(P.W, P.H, P.D));
-        setup_tiles += hdk::tiles_of(hdk::domain_cap_words(P.W, P.H, P.D));
+        setup_tiles += hdk::setup_tiles_of(P.W, P.H, P.D, setup_mode, bxw, by, bz);
     }
 
     // ---- uploads ----------------------------------------------------------
@@ -481,7 +482,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
                                  (unsigned long long*)(dbase + off_q[2])};
     if (timing) cudaEventRecord(ctx->ev[1], s);
     e = hdk::launch_setup(ddesc, n, setup_tiles, grid_setup, djobs, dstates, dq[g0 % 3], dctl, g0, bxw, by, bz,
-                          sh.kernel == 1 ? 1 : 0, s);
+                          setup_mode, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "setup launch");
     if (ro.map_a || ro.map_b) {
         e = hdk::launch_map_init(ddesc, ro.map_a, ro.map_b,

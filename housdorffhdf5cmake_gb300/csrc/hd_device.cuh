@@ -5,14 +5,22 @@
 //   a, b        uint8 masks, W x H x D, x fastest (caller's or staged copy)
 //   pa, pb      the full volume bit-packed along x: 32 voxels per uint32,
 //               bit i of word w of row (y, z) is voxel x = 32 w + i;
-//               row = wxf = ceil(W / 32) words, index (z * H + y) * wxf + w
+//               wxf = ceil(W / 32) words per row, rows padded with zero
+//               words to a multiple of 4 (packed_pitch), word w of row
+//               (y, z) at (z * H + y) * packed_pitch + w
 //   per direction (a "job": dilate a source mask until it covers a target):
 //     buf[0], buf[1]  ping-pong dilation state over the job's domain
-//     U               target voxels not yet covered
+//     U               target voxels not yet covered (one-step kernel; the
+//                     blocked kernel finds newly covered voxels as target
+//                     voxels in a step's result but not in its input)
 //               domain layout [z][y][pitch] words, pitch = ceil(wx / 4) * 4,
 //               pad words zero.  The domain is the bounding box of A u B with
 //               x widened to whole words (6-neighbour element) or the whole
-//               volume (18-neighbour element).
+//               volume (18-neighbour element).  The blocked kernel reads its
+//               first iteration's state and the target from the packed
+//               masks in place when the domain can start on a multiple of 4
+//               words without adding a brick column; else from crops of A
+//               and B in the domain layout (in the U slots of the two jobs).
 //   bricks      the unit of work of the persistent loop, one warp per brick:
 //               one-step kernel (hd_solve.cuh): BXW words (x) x (32 / BXW)
 //               rows (y) x BZ planes (z), lane (lx, ly) owns one word column
@@ -36,11 +44,11 @@ struct PairInfo {
 struct PairDesc {
     const uint8_t* a;
     const uint8_t* b;
-    uint32_t* pa;      // full packed A, wxf * H * D words
+    uint32_t* pa;      // full packed A, packed_pitch(W) * H * D words (16-byte aligned)
     uint32_t* pb;
     uint32_t* jb[2][3];  // per job: buf0, buf1, U (capacity: pitch_full * H * D words each)
     unsigned long long* hist[2];  // per job: kmax + 1 counters
-    int32_t W, H, D, wxf;
+    int32_t W, H, D, wxf;  // wxf = ceil(W / 32) words of a row (pitch: packed_pitch(W))
     int32_t se;          // 0: 6-neighbour, 1: 18-neighbour (forBench default)
     int32_t aligned;     // a and b are 16-byte aligned
     int32_t kmax;        // iteration cap per job
@@ -80,30 +88,63 @@ __host__ __device__ constexpr int tb_warp_bytes(int T, int BZ) {
 __host__ __device__ __forceinline__ long long pack_words(int W, int H, int D) {
     return (long long)((W + 31) / 32) * H * D;
 }
+// Row pitch of the packed volumes (words): 16-byte aligned rows.
+__host__ __device__ __forceinline__ int packed_pitch(int W) { return (((W + 31) / 32) + 3) & ~3; }
 __host__ __device__ __forceinline__ long long domain_cap_words(int W, int H, int D) {
     return (long long)((((W + 31) / 32) + 3) & ~3) * H * D;
 }
 __host__ __device__ __forceinline__ long long tiles_of(long long words) { return (words + kTileWords - 1) / kTileWords; }
+// Bricks of the full volume's brick grid (an upper bound of any domain's).
+__host__ __device__ __forceinline__ long long bricks_max(int W, int H, int D, int bxw, int by, int bz) {
+    return (long long)((((W + 31) / 32) + bxw - 1) / bxw) * ((H + by - 1) / by) * ((D + bz - 1) / bz);
+}
 
-// One direction of a pair, written by the set-up kernel.
-struct Job {
+// Set-up modes: what the dilation kernel will read (see setup_kernel).
+constexpr int kSetupBlocked = 0;         // blocked kernel: packed masks in place if that adds no brick column, else crops
+constexpr int kSetupOneStep = 1;         // one-step kernel: cropped ping-pong buffers and uncovered target
+constexpr int kSetupBlockedCrop = 2;     // blocked kernel: crops of A and B
+constexpr int kSetupBlockedInPlace = 3;  // blocked kernel: packed masks in place
+constexpr long long kSetupBricks = 2048; // bricks per set-up tile when nothing is copied
+
+// Set-up tiles of one pair: kTileWords words of the domain capacity when
+// the mode may copy, else kSetupBricks bricks of the largest brick grid.
+__host__ __device__ __forceinline__ long long setup_tiles_of(int W, int H, int D, int mode, int bxw, int by, int bz) {
+    if (mode != kSetupBlockedInPlace) return tiles_of(domain_cap_words(W, H, D));
+    const long long b = bricks_max(W, H, D, bxw, by, bz);
+    return b > 0 ? (b + kSetupBricks - 1) / kSetupBricks : 1;
+}
+
+// One direction of a pair, written by the set-up kernel.  The fields a
+// queue item of the blocked kernel reads come first, within one 128-byte
+// line (the rest serve the one-step kernel and instrumented runs).
+struct __align__(128) Job {
     uint32_t* buf[2];
-    uint32_t* U;
-    unsigned long long* hist;  // newly covered voxels per local step
-    int32_t wv, h, d;          // domain size in voxels
-    int32_t wx, pitch;         // words per row, row pitch (words)
+    // blocked kernel: the source (state of the first iteration) and the
+    // target, read-only: either the packed masks pa / pb read in place
+    // (domain rows start on 16-byte boundaries) or crops of them in the
+    // domain layout; domain word (x, y, z) is at
+    // vol + ((z + vz0) * vh + y + vy0) * vpitch + vx0 + x
+    const uint32_t* vol[2];
+    int32_t wx, h, d;          // domain: words per row, rows, planes
+    int32_t pitch;             // row pitch (words)
     uint32_t tailmask;         // valid bits of a row's last word
     int32_t nbx, nby, nbz;     // brick grid
     int32_t k0;                // global iteration at which local step 1 runs
     int32_t kmax;              // local step cap
+    uint32_t epoch;            // entries carrying another epoch belong to a previous user of the slot
+    int32_t vpitch, vh;        // vol[]: row pitch (words) and rows per plane
+    int32_t vx0, vy0, vz0;     // vol[]: domain origin (words, rows, planes)
+    unsigned long long brick0;
+    unsigned long long* hist;  // newly covered voxels per local step
+    // ---- one-step kernel, instrumented runs
+    uint32_t* U;
+    int32_t wv;                // domain width in voxels
     int32_t ox, oy, oz;        // domain origin in the full volume (voxels)
     int32_t tw, th;            // full-volume 32^3 tile grid (x, y), instrumented runs
-    unsigned long long brick0;
     int32_t* tstamp;           // instrumented runs: per full-volume tile, last marked step
     unsigned long long* tcount;  // instrumented runs: tiles per step
-    uint32_t epoch;            // entries carrying another epoch belong to a previous user of the slot
-    uint32_t pad_;
 };
+static_assert(__builtin_offsetof(Job, U) <= 128, "hot fields of a job within its first line");
 
 // Queue entry: epoch (8 bits) | job (24 bits) | local brick (32 bits).
 __host__ __device__ __forceinline__ unsigned long long make_entry(uint32_t epoch, uint32_t job, uint32_t lb) {

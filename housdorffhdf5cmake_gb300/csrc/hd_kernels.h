@@ -8,16 +8,15 @@
 
 namespace hdk {
 
-// Packing and set-up run over `ntiles` tiles of kTileWords words (descs[i].tile0
-// = first tile of pair i, increasing) with `grid` CTAs.  Brick geometry:
-// bxw words x by rows x bz planes (both kernel families).
+// Packing and set-up run over `ntiles` tiles (descs[i].tile0 / stile0 =
+// first tile of pair i, increasing; per pair tiles_of(pack_words) and
+// setup_tiles_of) with `grid` CTAs.  Brick geometry: bxw words x by rows x
+// bz planes (both kernel families).
 // label: 0 = every nonzero byte is foreground, 1..255 = bytes equal to label.
 cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, int grid, int label, cudaStream_t s);
-// init_second: also initialise each job's second ping-pong buffer (the
-// one-step kernel needs it; the blocked kernel writes it in its first step).
 cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int grid, Job* jobs,
                          JobState* states, unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
-                         int init_second, cudaStream_t s);
+                         int mode, cudaStream_t s);
 // Device-side decode of each pair's result into out[i] (asynchronous entry):
 // the same rules as the host decoder; robust HD at percentile pct.
 cudaError_t launch_finalize(const Ctl* ctl, const JobState* states, const PairDesc* d_descs, int npairs, float pct,

@@ -75,7 +75,7 @@ Layout plan(int W, int H, int D) {
     L.hist = take(2 * sizeof(unsigned long long) * (L.kmax + 1));
     for (auto& q : L.queue) q = take(sizeof(unsigned long long) * 2 * L.bricks);
     L.stamps = take(sizeof(int32_t) * 2 * L.bricks);
-    const size_t full = 4ull * L.wxf * H * D;
+    const size_t full = 4ull * hdk::packed_pitch(W) * H * D;
     L.pa = take(full);
     L.pb = take(full);
     for (int j = 0; j < 2; ++j)
@@ -216,7 +216,7 @@ extern "C" hd_status hd_compute_u8_device_noalloc(const uint8_t* d_a, const uint
     }
     const hdk::PairDesc* desc = (const hdk::PairDesc*)(base + L.desc);
     const long long ptiles = hdk::tiles_of(hdk::pack_words(W, H, D));
-    const long long stiles = hdk::tiles_of(hdk::domain_cap_words(W, H, D));
+    const long long stiles = hdk::setup_tiles_of(W, H, D, hdk::kSetupOneStep, kBxw, 32 / kBxw, kBz);
     const int cap_ctas = std::max(slot->sm_count * 8, 1);
     if (e == cudaSuccess)  // nonzero bytes are foreground
         e = hdk::launch_pack(desc, 1, ptiles, (int)std::min<long long>(cap_ctas, ptiles), 0, s);
@@ -227,7 +227,7 @@ extern "C" hd_status hd_compute_u8_device_noalloc(const uint8_t* d_a, const uint
                                 (unsigned long long*)(base + L.queue[2])};
     if (e == cudaSuccess)
         e = hdk::launch_setup(desc, 1, stiles, (int)std::min<long long>(cap_ctas, stiles), jobs, states, q[g0 % 3], ctl,
-                              g0, kBxw, 32 / kBxw, kBz, 1, s);  // one-step kernel: both ping-pong buffers
+                              g0, kBxw, 32 / kBxw, kBz, hdk::kSetupOneStep, s);
     if (e == cudaSuccess) {
         hdk::SolveParams sp{};
         sp.jobs = jobs;

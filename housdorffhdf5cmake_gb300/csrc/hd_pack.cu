@@ -4,11 +4,13 @@
 //               box of getMinMaxes (hello.cu:398-526): uint8 masks -> 32 voxels
 //               per uint32 along x (the prototype packs along z, :598-631),
 //               with |A|, |B|, |A n B| and the bounding box of A u B (x in
-//               whole words).  One pass over the bytes, 128-bit streaming loads.
-// setup_kernel  replaces firstMetaPrepareKernel (hello.cu:763-877): crops the
-//               packed masks to each job's domain, builds the uncovered-target
-//               words, writes the job descriptors and queues every brick of
-//               each job for its first step.
+//               whole words).  One pass over the bytes, 128-bit streaming
+//               loads; rows stored at a pitch of a multiple of 4 words.
+// setup_kernel  replaces firstMetaPrepareKernel (hello.cu:763-877): writes
+//               the job descriptors and queues every brick of each job for
+//               its first step; for the one-step kernel it also crops the
+//               packed masks to each job's domain and builds the
+//               uncovered-target words.
 // map_init_kernel  -1 / 0 initialisation of the optional per-voxel maps.
 #include <algorithm>
 #include <climits>
@@ -167,6 +169,7 @@ struct PackWalk {
     const uint8_t* src[2];
     const uint8_t* end[2];
     unsigned wxf, W, H, total;  // words per row, bytes per row, rows per plane, words of the pair
+    unsigned pitch, npad;       // packed row pitch (words): wxf rounded up to 4, npad zero words
     unsigned dq, dr;            // 32 words = dq rows + dr words
     uint32_t tail;              // valid bits of a row's last word
 };
@@ -179,6 +182,8 @@ __device__ __forceinline__ PackWalk make_walk(const PairDesc& P) {
     k.end[0] = P.a + nbytes;
     k.end[1] = P.b + nbytes;
     k.wxf = (unsigned)P.wxf;
+    k.pitch = (unsigned)packed_pitch(P.W);
+    k.npad = k.pitch - k.wxf;
     k.W = (unsigned)P.W;
     k.H = (unsigned)P.H;
     k.total = (unsigned)((long long)P.wxf * P.H * P.D);  // < 2^31 words
@@ -191,7 +196,8 @@ __device__ __forceinline__ PackWalk make_walk(const PairDesc& P) {
 
 // One tile of a pair, any width, alignment or memory kind (device or
 // host-mapped).  Warp v packs words w_lo + 128 v + 32 i + lane (i < 4) of
-// both masks.  Word t (row r, word w) holds the mask bytes [o, o + n) with
+// both masks (word t = row r, word w is stored at r * pitch + w; the row's
+// last word also zeroes the padding after it).  Word t holds the mask bytes [o, o + n) with
 // o = r W + 32 w, n = min(32, W - 32 w); with q = o rounded down to 16 and
 // s = o - q they lie in the 16-byte chunks at q, q + 16 and, if s + n > 32,
 // q + 32.  Rows are contiguous, so word t + 1 starts at o + n, and when
@@ -295,8 +301,14 @@ __device__ __forceinline__ void pack_tile(const PairDesc& P, const PackWalk& k, 
             out[m] = __funnelshift_r(lo[i][m], hi, sh) & (last ? k.tail : 0xffffffffu);
         }
         if (!kEdge || t < k.total) {
-            P.pa[t] = out[0];
-            P.pb[t] = out[1];
+            const size_t o = (size_t)rr[i] * k.pitch + wi;
+            P.pa[o] = out[0];
+            P.pb[o] = out[1];
+            if (last && k.npad) {  // the row's last word also writes its padding (1-3 words)
+                P.pa[o + 1] = P.pb[o + 1] = 0u;
+                if (k.npad > 1) P.pa[o + 2] = P.pb[o + 2] = 0u;
+                if (k.npad > 2) P.pa[o + 3] = P.pb[o + 3] = 0u;
+            }
             acc.add(out[0], out[1], (int)rr[i], (int)yy[i], (int)wi);
         }
     }
@@ -342,13 +354,15 @@ struct Domain {
     int ox, oy, oz, wv, h, d, wx0, wx, pitch;
 };
 
-__device__ __forceinline__ Domain make_domain(const PairDesc& P, const PairInfo& I) {
+__device__ __forceinline__ Domain make_domain(const PairDesc& P, const PairInfo& I, bool quad) {
     Domain m;
     if (P.se == 0) {
         // 6-neighbour element: every shortest path between two voxels of the
         // bounding box of A u B is monotone and stays in it, so cropping to it
-        // (x widened to whole words, still inside the volume) is exact.
-        m.wx0 = I.bb[0];  // word columns
+        // (or to any box inside the volume that contains it: x widened to
+        // whole words, or to a start on a multiple of 4 words when `quad`)
+        // is exact.
+        m.wx0 = quad ? (I.bb[0] & ~3) : I.bb[0];  // word columns
         const int wx1 = I.bb[1];
         m.ox = 32 * m.wx0;
         m.wv = min(P.W, 32 * (wx1 + 1)) - m.ox;
@@ -371,16 +385,37 @@ __device__ __forceinline__ Domain make_domain(const PairDesc& P, const PairInfo&
     return m;
 }
 
+// Blocked kernel: can the domain start on a multiple of 4 words (its rows
+// then start on 16-byte boundaries of the packed masks, which the kernel
+// reads in place) without adding a brick column?  The 18-neighbour domain
+// is the whole volume, which starts at word 0.
+__device__ __forceinline__ bool blocked_in_place(const PairDesc& P, const PairInfo& I) {
+    if (P.se != 0) return true;
+    const int w1 = I.bb[1] + 1;  // the domain's words end here (inside the volume)
+    return (w1 - I.bb[0] + 3) / 4 == (w1 - (I.bb[0] & ~3) + 3) / 4;
+}
+
 __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_pair, Job* jobs, JobState* states,
                                            unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
-                                           bool init_second);
+                                           int mode, unsigned* s_base);
 
-// 1D grid, block 256: CTAs stride over the tiles of all pairs; tile 0 of a
-// pair also writes its job descriptors.  A pair's tiles cover its full
-// volume's word count, an upper bound of its domain.
+// 1D grid, block 256: CTAs stride over the tiles of all pairs
+// (setup_tiles_of per pair); tile 0 of a pair also writes its job
+// descriptors.  Modes:
+//   kSetupOneStep         crop the packed masks into both ping-pong buffers
+//                         and the uncovered-target array of each job
+//   kSetupBlocked         the blocked kernel reads the packed masks in place
+//                         when blocked_in_place, else crops of A and B (one
+//                         pair: an extra brick column costs a whole
+//                         latency-bound first iteration more than the copy)
+//   kSetupBlockedCrop     crops of A and B (the packed masks are freed after
+//                         set-up)
+//   kSetupBlockedInPlace  the packed masks in place (batches: the copy costs
+//                         more than the extra bricks)
 __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__ descs, int npairs, long long ntiles,
                                                     Job* jobs, JobState* states, unsigned long long* queue0,
-                                                    Ctl* ctl, int g0, int bxw, int by, int bz, int init_second) {
+                                                    Ctl* ctl, int g0, int bxw, int by, int bz, int mode) {
+    __shared__ unsigned s_base;
     int pi = -1;
     // CTAs stride over the tiles: a pair's domain fills only the first of
     // its tiles, so contiguous runs would leave some CTAs without work
@@ -388,18 +423,18 @@ __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__
         int np = pi < 0 ? pair_of_tile(descs, npairs, tile, true) : pi;
         while (np + 1 < npairs && descs[np + 1].stile0 <= tile) ++np;  // tiles only increase
         pi = np;
-        setup_tile(descs[pi], tile - descs[pi].stile0, jobs, states, queue0, ctl, g0, bxw, by, bz, init_second != 0);
+        setup_tile(descs[pi], tile - descs[pi].stile0, jobs, states, queue0, ctl, g0, bxw, by, bz, mode, &s_base);
     }
 }
 
 __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_pair, Job* jobs, JobState* states,
                                            unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
-                                           bool init_second) {
+                                           int mode, unsigned* s_base) {
     const PairInfo I = *P.info;
     const bool empty_a = I.n_a == 0, empty_b = I.n_b == 0;
     const unsigned long long rem[2] = {I.n_b - I.n_ab, I.n_a - I.n_ab};
-    const long long cap = domain_cap_words(P.W, P.H, P.D);  // this pair's tiles cover [0, cap) words
-    const long long ntiles_pair = tiles_of(cap);
+    const long long cap = domain_cap_words(P.W, P.H, P.D);  // copying modes: the tiles cover [0, cap) words
+    const long long ntiles_pair = setup_tiles_of(P.W, P.H, P.D, mode, bxw, by, bz);
     const long long w_lo = tile_in_pair * kTileWords, w_hi = min(cap, w_lo + kTileWords);
     const long long tid0 = threadIdx.x;
     const long long nthr = blockDim.x;
@@ -423,15 +458,34 @@ __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_
         }
         return;
     }
-    const Domain m = make_domain(P, I);
+    const bool one_step = mode == kSetupOneStep;
+    const bool in_place = mode == kSetupBlockedInPlace || (mode == kSetupBlocked && blocked_in_place(P, I));
+    const Domain m = make_domain(P, I, in_place);
     const int nbx = (m.wx + bxw - 1) / bxw, nby = (m.h + by - 1) / by, nbz = (m.d + bz - 1) / bz;
     const long long nbricks = (long long)nbx * nby * nbz;
+    // crops of A and B (blocked kernel) live in the two jobs' U slots
+    uint32_t* const crop[2] = {P.jb[0][2], P.jb[1][2]};
     if (first && tid0 == 0) {
         for (int j = 0; j < 2; ++j) {
             Job& J = jobs[P.job0 + j];
             J.buf[0] = P.jb[j][0];
             J.buf[1] = P.jb[j][1];
-            J.U = P.jb[j][2];
+            J.U = one_step ? P.jb[j][2] : nullptr;
+            if (in_place) {
+                J.vol[0] = j == 0 ? P.pa : P.pb;
+                J.vol[1] = j == 0 ? P.pb : P.pa;
+                J.vpitch = packed_pitch(P.W);
+                J.vh = P.H;
+                J.vx0 = m.wx0;
+                J.vy0 = m.oy;
+                J.vz0 = m.oz;
+            } else {
+                J.vol[0] = crop[j];
+                J.vol[1] = crop[1 - j];
+                J.vpitch = m.pitch;
+                J.vh = m.h;
+                J.vx0 = J.vy0 = J.vz0 = 0;
+            }
             J.hist = P.hist[j];
             J.wv = m.wv; J.h = m.h; J.d = m.d;
             J.wx = m.wx; J.pitch = m.pitch;
@@ -453,10 +507,9 @@ __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_
         }
     }
     // Crop copy.  Job 0 dilates A and must cover B; job 1 dilates B and covers A.
-    // buf[1] is written only for the one-step kernel: the blocked kernel's
-    // first iteration processes every brick and writes all of buf[1].
-    const long long words = min((long long)m.pitch * m.h * m.d, w_hi);
     const bool act0 = rem[0] > 0, act1 = rem[1] > 0;
+    const long long words = (one_step || !in_place) ? min((long long)m.pitch * m.h * m.d, w_hi) : 0;
+    const int vpitch = packed_pitch(P.W);
     for (long long t = w_lo + tid0; t < words; t += nthr) {
         // domain word index < 2^31: 32-bit divisions
         const unsigned tu = (unsigned)t;
@@ -466,42 +519,42 @@ __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_
         if (w < m.wx) {
             const unsigned zq = r / (unsigned)m.h;
             const int yl = (int)(r - zq * (unsigned)m.h), zl = (int)zq;
-            const long long src = ((long long)(m.oz + zl) * P.H + (m.oy + yl)) * P.wxf + m.wx0 + w;
+            const long long src = ((long long)(m.oz + zl) * P.H + (m.oy + yl)) * vpitch + m.wx0 + w;
             a = __ldg(P.pa + src);
             b = __ldg(P.pb + src);
         }
-        if (act0) {
-            P.jb[0][0][t] = a;
-            if (init_second) P.jb[0][1][t] = a;
-            P.jb[0][2][t] = b & ~a;
-        }
-        if (act1) {
-            P.jb[1][0][t] = b;
-            if (init_second) P.jb[1][1][t] = b;
-            P.jb[1][2][t] = a & ~b;
+        if (one_step) {
+            if (act0) {
+                P.jb[0][0][t] = a;
+                P.jb[0][1][t] = a;
+                P.jb[0][2][t] = b & ~a;
+            }
+            if (act1) {
+                P.jb[1][0][t] = b;
+                P.jb[1][1][t] = b;
+                P.jb[1][2][t] = a & ~b;
+            }
+        } else {  // source and target of both jobs
+            crop[0][t] = a;
+            crop[1][t] = b;
         }
     }
-    // First step of each active job: every brick of its domain (one
-    // warp-aggregated append per 32 bricks).
-    // the bricks are split evenly over the pair's tiles
-    const int lane = threadIdx.x & 31;
-    const long long gwarp = tid0 >> 5, nwarps = nthr >> 5;
-    // < 2^31 bricks and tiles per pair: 32-bit division
-    const long long b_per = (long long)(((unsigned)nbricks + (unsigned)ntiles_pair - 1u) / (unsigned)ntiles_pair);
+    // First step of each active job: every brick of its domain.  The
+    // bricks go to the pair's first tiles, at least 256 per tile, and each
+    // such tile reserves its queue entries with one atomic per job.
+    const long long b_even = (long long)(((unsigned)nbricks + (unsigned)ntiles_pair - 1u) / (unsigned)ntiles_pair);
+    const long long b_per = mode == kSetupBlockedInPlace ? kSetupBricks
+                                                          : (b_even > 256 ? b_even : 256);  // < 2^31 bricks, tiles
     const long long b_lo = tile_in_pair * b_per, b_hi = min(nbricks, b_lo + b_per);
+    if (b_lo >= b_hi) return;  // CTA-uniform
     for (int j = 0; j < 2; ++j) {
         if (!(j == 0 ? act0 : act1)) continue;
-        for (long long b0 = b_lo + gwarp * 32; b0 < b_hi; b0 += nwarps * 32) {
-            const long long t = b0 + lane;
-            const bool have = t < b_hi;
-            const unsigned mball = __ballot_sync(0xffffffffu, have);
-            unsigned base = 0;
-            if (lane == 0) base = atomicAdd(&ctl->qcount[g0 % 3], (unsigned)__popc(mball));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (have)
-                queue0[base + __popc(mball & ((1u << lane) - 1u))] =
-                    make_entry(P.epoch, (uint32_t)(P.job0 + j), (uint32_t)t);
-        }
+        if (tid0 == 0) *s_base = atomicAdd(&ctl->qcount[g0 % 3], (unsigned)(b_hi - b_lo));
+        __syncthreads();
+        const unsigned base = *s_base;
+        for (long long t = b_lo + tid0; t < b_hi; t += nthr)
+            queue0[base + (unsigned)(t - b_lo)] = make_entry(P.epoch, (uint32_t)(P.job0 + j), (uint32_t)t);
+        __syncthreads();  // s_base is written again next
     }
 }
 
@@ -635,11 +688,10 @@ cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, i
 
 cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int grid, Job* jobs,
                          JobState* states, unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
-                         int init_second, cudaStream_t s) {
+                         int mode, cudaStream_t s) {
     if (grid > ntiles) grid = (int)ntiles;
     if (grid < 1) grid = 1;
-    setup_kernel<<<grid, 256, 0, s>>>(d_descs, npairs, ntiles, jobs, states, queue0, ctl, g0, bxw, by, bz,
-                                      init_second);
+    setup_kernel<<<grid, 256, 0, s>>>(d_descs, npairs, ntiles, jobs, states, queue0, ctl, g0, bxw, by, bz, mode);
     return cudaGetLastError();
 }
 

@@ -118,7 +118,7 @@ struct hd_server {
     std::vector<Request*> slots;      // resident pair per slot
     std::vector<int> free_slots;
     std::vector<int> quarantine;      // slots freed during the last tick
-    std::vector<uint32_t> slot_epoch; // bumped on every admission into a slot
+    std::vector<uint32_t> slot_epoch; // bumped on every admission into a slot and on every completion
     RangeAlloc bricks;
     unsigned long long brick_cap = 0;
     // persistent device state
@@ -147,21 +147,24 @@ hd_status cuda_err(hd_server* s, cudaError_t e, const char* where) {
 }
 
 // Sizes of one request's device memory (resident part lives until completion,
-// transient part only through packing and set-up).
+// transient part only through packing and set-up).  Resident: three
+// domain-sized buffers per job (both ping-pong buffers, and the
+// uncovered-target array of the one-step kernel or a crop of one mask for
+// the blocked kernel), histograms, counts.  Transient: the packed masks and
+// the staged host masks.
 void plan_request(hd_server* s, Request* r) {
     const int by = s->shape.by;
     r->wxf = (r->W + 31) / 32;
     const long long pitch = (r->wxf + 3) / 4 * 4;
     r->dom_words = pitch * r->H * r->D;
-    r->nbricks = (unsigned long long)((r->wxf + s->shape.bxw - 1) / s->shape.bxw) * ((r->H + by - 1) / by) *
-                 ((r->D + s->shape.bz - 1) / s->shape.bz);
+    r->nbricks = (unsigned long long)hdk::bricks_max(r->W, r->H, r->D, s->shape.bxw, by, s->shape.bz);
     r->kmax = r->W + r->H + r->D;
     const size_t job_bytes = align_up(4ULL * r->dom_words);
     r->off_hist = 6 * job_bytes;
     r->off_info = align_up(r->off_hist + 2ULL * (r->kmax + 1) * sizeof(uint64_t));
     r->resident_bytes = align_up(r->off_info + sizeof(PairInfo));
     const size_t nb = (size_t)r->W * r->H * r->D;
-    const size_t packed = align_up(4ULL * r->wxf * r->H * r->D);
+    const size_t packed = align_up(4ULL * hdk::packed_pitch(r->W) * r->H * r->D);
     r->transient_bytes = 2 * packed + (r->dev_a ? 0 : 2 * align_up(nb));
 }
 
@@ -224,6 +227,8 @@ void tick(hd_server* s) {
     std::vector<PairDesc> descs;
     std::vector<Request*> admitted;
     long long ptiles = 0, stiles = 0;
+    // the packed masks are freed after set-up: the blocked kernel reads crops
+    const int setup_mode = s->shape.kernel == 1 ? hdk::kSetupOneStep : hdk::kSetupBlockedCrop;
     for (size_t i = 0; i < admit.size(); ++i) {
         Request* r = admit[i];
         void* res = nullptr;
@@ -246,7 +251,7 @@ void tick(hd_server* s) {
         char* rb = (char*)res;
         char* tb = (char*)tr;
         const size_t nb = (size_t)r->W * r->H * r->D;
-        const size_t packed = align_up(4ULL * r->wxf * r->H * r->D);
+        const size_t packed = align_up(4ULL * hdk::packed_pitch(r->W) * r->H * r->D);
         PairDesc d{};
         if (r->dev_a) {
             d.a = r->dev_a;
@@ -279,7 +284,7 @@ void tick(hd_server* s) {
         d.tile0 = ptiles;
         d.stile0 = stiles;
         ptiles += hdk::tiles_of(hdk::pack_words(r->W, r->H, r->D));
-        stiles += hdk::tiles_of(hdk::domain_cap_words(r->W, r->H, r->D));
+        stiles += hdk::setup_tiles_of(r->W, r->H, r->D, setup_mode, s->shape.bxw, s->shape.by, s->shape.bz);
         d.info = (PairInfo*)(rb + r->off_info);
         descs.push_back(d);
         admitted.push_back(r);
@@ -298,7 +303,7 @@ void tick(hd_server* s) {
             e = hdk::launch_setup(s->d_descs, (int)admitted.size(), stiles, (int)std::min<long long>(cap_ctas, stiles),
                                   s->d_jobs, s->d_states,
                                   s->d_queue[s->g_next % 3], s->d_ctl, s->g_next, s->shape.bxw, s->shape.by,
-                                  s->shape.bz, s->shape.kernel == 1 ? 1 : 0, st);
+                                  s->shape.bz, setup_mode, st);
         // no wait here: the host masks' copies read the requests' own
         // buffers (alive until completion), the descriptors' staging area is
         // rewritten only after the end-of-tick synchronisation, and the
@@ -407,6 +412,12 @@ void tick(hd_server* s) {
                 st_r = decode_result(info, s0, s1, hist.data() + kp1, hist.data(), kp1, 0, hard_err, pct, &r->result);
             }
         }
+        // Queue entries of the finished jobs may still be waiting for the
+        // next step: a new epoch on the jobs makes the kernels drop them
+        // before they read the buffers freed here (the byte fills the whole
+        // epoch word; entries compare its low 8 bits).
+        const unsigned dead = ++s->slot_epoch[sl] & 0xffu;
+        for (int j = 0; j < 2; ++j) cudaMemsetAsync(&s->d_jobs[2 * sl + j].epoch, (int)dead, sizeof(uint32_t), st);
         cudaFreeAsync(r->resident, st);
         r->resident = nullptr;
         std::lock_guard<std::mutex> lk(s->mu);

@@ -90,15 +90,23 @@ struct TbItem {
     bool live;
 };
 
-// Where this lane's row of a streamed plane comes from.
+// Where this lane's row of a streamed plane comes from: domain plane z, row
+// y, words wx0 .. wx0 + 3 of the brick are at src + (z + zoff) * plane +
+// rowoff.  The level-0 state is the job's ping-pong buffer, except in the
+// job's first iteration, which reads the source (vol[0]); the target always
+// comes from vol[1].  Every row copy is one 16-byte copy: the domain layout
+// and the packed masks (rows padded to a multiple of 4 words, read in place
+// only when the domain starts on a multiple of 4 words) keep a brick's 4
+// words in its row, and those past the domain are row padding or outside
+// the bounding box of A u B (zero).
 struct TbRow {
-    const uint32_t* src;  // level-0 state of the job (this item's ping-pong buffer)
-    int plane, rowoff, z0, Dd;
+    const uint32_t* src;
+    int plane, rowoff, zoff, z0, Dd;
     bool rowv, hl_ok, hr_ok;
 };
 
 template <int T, int BZ>
-__device__ __forceinline__ TbRow tb_row(const TbItem& it) {
+__device__ __forceinline__ TbRow tb_row(const TbItem& it, bool target) {
     constexpr int IW = 4;
     constexpr int BYI = 32 - 2 * T;
     const int lane = threadIdx.x & 31;
@@ -108,9 +116,18 @@ __device__ __forceinline__ TbRow tb_row(const TbItem& it) {
     const int wx0 = it.bx * IW;
     const int y = it.by * BYI - T + lane;
     w.rowv = y >= 0 && y < Hd;
-    w.src = Jp->buf[it.iter & 1];
-    w.plane = Jp->pitch * Hd;
-    w.rowoff = (w.rowv ? y : 0) * Jp->pitch + wx0;
+    const int yc = w.rowv ? y : 0;
+    if (target || it.iter == 0) {
+        w.src = Jp->vol[target ? 1 : 0];
+        w.plane = Jp->vpitch * Jp->vh;
+        w.rowoff = (yc + Jp->vy0) * Jp->vpitch + Jp->vx0 + wx0;
+        w.zoff = Jp->vz0;
+    } else {
+        w.src = Jp->buf[it.iter & 1];
+        w.plane = Jp->pitch * Hd;
+        w.rowoff = yc * Jp->pitch + wx0;
+        w.zoff = 0;
+    }
     w.z0 = it.bz * BZ;
     w.Dd = Jp->d;
     w.hl_ok = w.rowv && wx0 > 0;
@@ -126,7 +143,7 @@ __device__ __forceinline__ void tb_copy_plane(const TbRow& w, int r, unsigned ch
     const int lane = threadIdx.x & 31;
     const int z = w.z0 - T + r;
     const bool ok = w.rowv && z >= 0 && z < w.Dd;
-    const uint32_t* gp = w.src + (ok ? z * w.plane + w.rowoff : 0);
+    const uint32_t* gp = w.src + (ok ? (z + w.zoff) * w.plane + w.rowoff : 0);
     const int slot = r % SM::R;
     const uint32_t base = (uint32_t)__cvta_generic_to_shared(wsm);
     const uint32_t s_in = base + (uint32_t)((slot * 32 + lane) * 16);
@@ -158,8 +175,9 @@ __device__ __forceinline__ bool tb_decode(const SolveParams& p, unsigned long lo
     it.active = ld_relaxed_s32(&it.st->active);
     const uint32_t jep = Jp->epoch;
     const int k0 = Jp->k0, kmax = Jp->kmax, nbx = Jp->nbx, nby = Jp->nby;
-    // touched here so that the issue and compute phases find them in L1
-    const int warm = Jp->wx + Jp->h + Jp->d + Jp->pitch + (int)Jp->tailmask;
+    // one load per 32-byte sector of the job's first line, so that the
+    // issue and compute phases find its fields in L1
+    const int warm = (int)(size_t)Jp->vol[1] + Jp->wx + Jp->vpitch + (int)(size_t)Jp->hist;
     asm volatile("" ::"r"(warm));
     if ((jep & 0xffu) != it.epoch) return false;  // left over from the slot's previous pair
     it.iter = g - k0;
@@ -180,25 +198,28 @@ __device__ __forceinline__ bool tb_decode(const SolveParams& p, unsigned long lo
 }
 
 // Decodes a queue entry (tb_decode) and issues the copies of the brick's
-// uncovered-target rows (one group) and of its first planes (one group
-// each).  No wait.
+// target rows (one group) and of its first planes (one group each).  No
+// wait.
 template <int T, int BZ>
 __device__ __forceinline__ void tb_issue(const SolveParams& p, unsigned long long e, int g, unsigned char* wsm,
                                          TbItem& it) {
     using SM = TbSmem<T, BZ>;
     const int lane = threadIdx.x & 31;
     if (!tb_decode<T>(p, e, g, it)) return;
-    const Job* Jp = it.Jp;
-    const TbRow w = tb_row<T, BZ>(it);
-    const bool inter = w.rowv && lane >= T && lane < 32 - T;
-    const uint32_t s_u = (uint32_t)__cvta_generic_to_shared(wsm) + SM::kUOff;
+    {
+        const TbRow t = tb_row<T, BZ>(it, true);
+        const bool inter = t.rowv && lane >= T && lane < 32 - T;
+        const uint32_t s_u = (uint32_t)__cvta_generic_to_shared(wsm) + SM::kUOff;
 #pragma unroll
-    for (int i = 0; i < BZ; ++i) {
-        const int z = w.z0 + i;
-        const bool ok = inter && z < w.Dd;
-        cp_async16(s_u + (uint32_t)((i * 32 + lane) * 16), Jp->U + (ok ? z * w.plane + w.rowoff : 0), ok ? 16u : 0u);
+        for (int i = 0; i < BZ; ++i) {
+            const int z = t.z0 + i;
+            const bool ok = inter && z < t.Dd;
+            cp_async16(s_u + (uint32_t)((i * 32 + lane) * 16), t.src + (ok ? (z + t.zoff) * t.plane + t.rowoff : 0),
+                       ok ? 16u : 0u);
+        }
+        cp_async_commit();
     }
-    cp_async_commit();
+    const TbRow w = tb_row<T, BZ>(it, false);
 #pragma unroll
     for (int r = 0; r < SM::PF && r < SM::NP; ++r) tb_copy_plane<T, BZ>(w, r, wsm);
 }
@@ -213,7 +234,12 @@ struct TbOut {
 
 // Runs the item's T steps plane by plane, copying planes into the ring PF
 // ahead (per level the pending plane's partial result and the last plane's Z
-// stay in registers), and writes its state and uncovered-target words back.
+// stay in registers), and writes its state back (in the job's first
+// iteration to both ping-pong buffers: a brick that is not queued for the
+// next iteration must find its state in either).  The state only grows, so
+// the target voxels a step covers are those in its result and not in its
+// input: the 6-neighbour element finds the input plane in registers, the
+// 18-neighbour element keeps target minus state per row in shared memory.
 // An item whose job finished since it was issued is dropped here.
 template <int T, int BZ, bool SE18>
 __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& it, unsigned char* wsm, TbOut& res) {
@@ -230,12 +256,14 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
         cp_async_wait<0>();
         return;
     }
-    const TbRow w = tb_row<T, BZ>(it);
+    const TbRow w = tb_row<T, BZ>(it, false);
     const int Wx = Jp->wx;
     const int wx0 = it.bx * IW;
     const bool inter = w.rowv && lane >= T && lane < 32 - T;
     uint32_t* __restrict__ dst = Jp->buf[(it.iter + 1) & 1];
-    uint32_t* __restrict__ U = Jp->U;
+    uint32_t* __restrict__ dst2 = it.iter == 0 ? Jp->buf[0] : nullptr;
+    const int bplane = Jp->pitch * Jp->h;
+    const int browoff = (w.rowv ? it.by * BYI - T + lane : 0) * Jp->pitch + wx0;
     uint32_t wm[NW];  // valid bits of each word of this lane's row
     {
         uint32_t w6[IW + 2];
@@ -304,7 +332,7 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
 #pragma unroll
         for (int j = 0; j < NW; ++j) acc[s][j] = zp[s][j] = 0u;
     }
-    uint32_t d_any = 0, d_xl = 0, d_xh = 0, d_zl = 0, d_zh = 0, u_hits = 0;
+    uint32_t d_any = 0, d_xl = 0, d_xh = 0, d_zl = 0, d_zh = 0;
     const bool band_yl = inter && (lane - T) < T;
     const bool band_yh = inter && (lane - T) >= BYI - T;
     (void)p;
@@ -331,8 +359,12 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
         for (int s = 1; s <= T; ++s) {
             const int r = q - s;
             uint32_t out[NW];
+            // 6-neighbour element: a plane's z term is the plane itself, so
+            // zp[s - 1] holds plane r at level s - 1 until it is replaced here
+            uint32_t prev[NW];
 #pragma unroll
             for (int j = 0; j < NW; ++j) {
+                if constexpr (!SE18) prev[j] = zp[s - 1][j];
                 out[j] = acc[s - 1][j] | Z[j];
                 acc[s - 1][j] = M[j] | zp[s - 1][j];
                 zp[s - 1][j] = Z[j];
@@ -351,10 +383,26 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
                 for (int j = 0; j < NW; ++j) out[j] = pv ? (out[j] & wm[j]) : 0u;
             }
             if (r >= T && r < T + BZ) {
-                // cover test of the interior at step kb + s (U rows of
-                // non-interior lanes and planes are zero)
+                // cover test of the interior at step kb + s (target rows of
+                // non-interior lanes and planes are zero).  The state only
+                // grows, so the voxels step kb + s covers are the target
+                // voxels in plane r at level s but not at level s - 1.
                 uint32_t* ur = u_row(r - T);
                 uint4 u = *reinterpret_cast<const uint4*>(ur);
+                if constexpr (!SE18) {
+                    u.x &= ~prev[1];
+                    u.y &= ~prev[2];
+                    u.z &= ~prev[3];
+                    u.w &= ~prev[4];
+                } else if (s == 1) {
+                    // the 18-neighbour z term is not the plane: the row keeps
+                    // the uncovered target, target minus the level-0 state
+                    const uint4 c0 = in_row(r);
+                    u.x &= ~c0.x;
+                    u.y &= ~c0.y;
+                    u.z &= ~c0.z;
+                    u.w &= ~c0.w;
+                }
                 const uint32_t h0 = out[1] & u.x, h1 = out[2] & u.y, h2 = out[3] & u.z, h3 = out[4] & u.w;
                 const uint32_t hany = h0 | h1 | h2 | h3;
                 if (hany) {
@@ -363,26 +411,28 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
                     u.y &= ~h1;
                     u.z &= ~h2;
                     u.w &= ~h3;
-                    *reinterpret_cast<uint4*>(ur) = u;
-                    u_hits |= 1u << (r - T);
+                }
+                if constexpr (SE18) {
+                    if (s < T && (s == 1 || hany))  // the last level reads the row for the last time
+                        *reinterpret_cast<uint4*>(ur) = u;
                 }
             }
             if (s < T) {
                 terms(out, M, Z);  // level s terms of plane r, for level s + 1
             } else {
-                // final level: store, write back U, record changes
+                // final level: store, record changes
                 const int z = w.z0 - T + r;
                 if (inter && z < w.Dd) {
-                    const int off = z * w.plane + w.rowoff;
-                    *reinterpret_cast<uint4*>(dst + off) = make_uint4(out[1], out[2], out[3], out[4]);
+                    const int off = z * bplane + browoff;
+                    const uint4 o4 = make_uint4(out[1], out[2], out[3], out[4]);
+                    *reinterpret_cast<uint4*>(dst + off) = o4;
+                    if (dst2) *reinterpret_cast<uint4*>(dst2 + off) = o4;
                     const uint4 c0 = in_row(r);
                     const uint32_t dx0 = out[1] ^ (c0.x & wm[1]), dx3 = out[4] ^ (c0.w & wm[4]);
                     const uint32_t dall = dx0 | (out[2] ^ (c0.y & wm[2])) | (out[3] ^ (c0.z & wm[3])) | dx3;
                     // only changes within T voxels of an x face can reach
                     // the x neighbour's interior during its next T steps
                     constexpr uint32_t kLoBits = (1u << T) - 1u, kHiBits = ~(0xffffffffu >> T);
-                    if (u_hits & (1u << (r - T)))
-                        *reinterpret_cast<uint4*>(U + off) = *reinterpret_cast<const uint4*>(u_row(r - T));
                     d_any |= dall;
                     d_xl |= dx0 & kLoBits;
                     d_xh |= dx3 & kHiBits;

@@ -165,6 +165,41 @@ def test_host_device_and_zero_copy_paths(hd, ctx, oracle):
     assert_same(ctx.compute(va, vb, "se6"), o, "unaligned device")
 
 
+# x extents (first, last word) of A u B: the blocked kernel reads the packed
+# masks in place when its domain can start on a multiple of 4 words without
+# an extra brick column (e.g. words 2-3, 4-6), else crops of A and B (words
+# 1-4, 3-4); batches always read in place.
+WORD_EXTENTS = [(0, 0), (1, 4), (2, 3), (3, 3), (3, 4), (4, 6), (5, 7), (1, 7), (6, 6)]
+
+
+def _pair_in_words(rng, shape, w0, w1):
+    D, H, W = shape
+    x0, x1 = 32 * w0, min(W, 32 * (w1 + 1)) - 1
+    a = np.zeros(shape, np.uint8)
+    b = np.zeros(shape, np.uint8)
+    for m, p in ((a, 0.03), (b, 0.02)):
+        m[:, :, x0:x1 + 1] = rng.random((D, H, x1 - x0 + 1)) < p
+    a[D // 2, H // 3, x0] = 1  # both ends of the extent
+    b[D // 3, H // 2, x1] = 1
+    return a, b
+
+
+@pytest.mark.parametrize("metric", ["se6", "se18"])
+@pytest.mark.parametrize("width", [256, 200])
+def test_blocked_domain_origins(hd, oracle, metric, width):
+    rng = np.random.default_rng(width)
+    shape = (12, 40, width)
+    pairs = [_pair_in_words(rng, shape, w0, w1) for w0, w1 in WORD_EXTENTS if 32 * w0 < width]
+    want = [oracle.forbench(a, b, metric) for a, b in pairs]
+    for steps in (1, 4):
+        with hd.Context(0, kernel=2, steps_per_barrier=steps) as c:
+            for (a, b), o, ext in zip(pairs, want, WORD_EXTENTS):
+                assert_same(c.compute(cuda(a), cuda(b), metric), o, f"words {ext} steps {steps}")
+            got = c.batch([(cuda(a), cuda(b)) for a, b in pairs], metric)
+            for g, o, ext in zip(got, want, WORD_EXTENTS):
+                assert_same(g, o, f"batch words {ext} steps {steps}")
+
+
 def test_batch_equals_plain(ctx, oracle):
     specs = synth.batch_ragged_specs(3, n=24, lo=16, hi=80, edge_frac=0.2)
     pairs = [synth.pair_from_spec(s) for s in specs]
