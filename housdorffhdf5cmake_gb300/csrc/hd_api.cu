@@ -510,17 +510,21 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     if (occ <= 0) return set_error(ctx, HD_ERR_CUDA, "dilation kernel cannot be made resident");
     const int per_sm = cps > 0 ? std::min(cps, occ) : occ;
     dim3 grid(ctx->sm_count * per_sm), block(sh.threads);
+    const float pct = (ctx->opt.percentile > 0.f && ctx->opt.percentile <= 1.f) ? ctx->opt.percentile : 0.95f;
+    if (async) {  // the launch decodes the results on the device
+        sp.descs = ddesc;
+        sp.npairs = n;
+        sp.pct = pct;
+        sp.out = ro.async_out;
+    }
     void* args[] = {&sp};
     if (timing) cudaEventRecord(ctx->ev[2], s);
     e = cudaLaunchCooperativeKernel(solve_fn, grid, block, args, (size_t)sh.smem, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "dilation launch");
     if (timing) cudaEventRecord(ctx->ev[3], s);
-    const float pct = (ctx->opt.percentile > 0.f && ctx->opt.percentile <= 1.f) ? ctx->opt.percentile : 0.95f;
     if (async) {
-        // decode on the device; the step counter moves past any step this
-        // launch can reach (its stamps stay below the next call's steps)
-        e = hdk::launch_finalize(dctl, dstates, ddesc, n, pct, ro.async_out, s);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "result decode launch");
+        // the step counter moves past any step this launch can reach (its
+        // stamps stay below the next call's steps)
         ctx->g_next = g0 + sp.max_iters + 2;
         return HD_OK;
     }

@@ -29,6 +29,8 @@
 #pragma once
 #include <stdint.h>
 
+#include "hd/hd.h"
+
 namespace hdk {
 
 constexpr int kMaxPairsPerLaunch = 65535;
@@ -189,6 +191,12 @@ struct SolveParams {
     int32_t max_iters;             // iterations this launch may run
     int32_t stats;                 // instrumented run
     long long timeout_ns;          // one barrier wait
+    // device-side result decode at the end of the launch (asynchronous
+    // entries; out == nullptr: the host decodes)
+    const PairDesc* descs;
+    int32_t npairs;
+    float pct;                     // robust HD percentile
+    hd_result* out;                // out[i] = result of pair i
 };
 
 }  // namespace hdk

@@ -118,56 +118,6 @@ __global__ void noalloc_prepare(unsigned char* base, Layout L, const uint8_t* a,
     P->stile0 = 0;
 }
 
-// Device-side counterpart of the host result decoding: counts, sums, HD,
-// average (one double division) and the 95th-percentile HD with the float
-// stopping rule of hello.cu:1751-1758.
-__device__ int robust_k_dev(const unsigned long long* hist, int len, unsigned long long total, float p) {
-    const float tf = (float)total * p;
-    unsigned long long cov = 0;
-    for (int k = 0; k < len; ++k) {
-        if (k > 0) cov += hist[k];
-        if (!(tf > (float)cov)) return k;
-    }
-    return len - 1;
-}
-
-__global__ void noalloc_finalize(const unsigned char* base, Layout L, hd_result* out) {
-    const hdk::Ctl* ctl = (const hdk::Ctl*)(base + L.ctl);
-    const hdk::JobState* st = (const hdk::JobState*)(base + L.states);
-    const hdk::PairInfo* I = (const hdk::PairInfo*)(base + L.info);
-    const unsigned long long* hist = (const unsigned long long*)(base + L.hist);
-    hd_result r;
-    memset(&r, 0, sizeof r);
-    r.n_a = I->n_a;
-    r.n_b = I->n_b;
-    r.n_a_not_b = I->n_a - I->n_ab;
-    r.n_b_not_a = I->n_b - I->n_ab;
-    r.iterations = ctl->iters_run;
-    if (I->n_a == 0 && I->n_b == 0) {
-        r.status = HD_OK;
-    } else if (I->n_a == 0 || I->n_b == 0) {
-        r.status = HD_EMPTY_MASK;
-        r.hd = r.hd_ab = r.hd_ba = r.hd_robust = -1;
-        r.avg_hd = __longlong_as_double(0x7ff8000000000000LL);
-    } else {
-        int s = ctl->err;
-        if (!s) s = st[0].status ? st[0].status : st[1].status;
-        if (!s && (st[0].remaining != 0 || st[1].remaining != 0)) s = HD_ERR_ITER_LIMIT;
-        r.status = s;
-        r.hd_ba = st[0].hd;
-        r.sum_ba = st[0].sum;
-        r.hd_ab = st[1].hd;
-        r.sum_ab = st[1].sum;
-        r.hd = max(r.hd_ab, r.hd_ba);
-        r.avg_hd = (double)(r.sum_ab + r.sum_ba) / (double)(r.n_a + r.n_b);
-        const int kp1 = L.kmax + 1;
-        r.hd_robust = max(robust_k_dev(hist + kp1, kp1, r.n_a_not_b, 0.95f),
-                          robust_k_dev(hist, kp1, r.n_b_not_a, 0.95f));
-        if (s != HD_OK) r.hd = r.hd_ab = r.hd_ba = r.hd_robust = -1;
-    }
-    *out = r;
-}
-
 }  // namespace
 
 extern "C" hd_status hd_compute_u8_device_noalloc(const uint8_t* d_a, const uint8_t* d_b, int32_t W, int32_t H,
@@ -241,13 +191,13 @@ extern "C" hd_status hd_compute_u8_device_noalloc(const uint8_t* d_a, const uint
         sp.g0 = g0;
         sp.max_iters = L.kmax + 2;
         sp.timeout_ns = 10000000000LL;
+        sp.descs = desc;  // the launch decodes the result into d_out
+        sp.npairs = 1;
+        sp.pct = 0.95f;
+        sp.out = d_out;
         void* args[] = {&sp};
         e = cudaLaunchCooperativeKernel(solve, dim3(slot->sm_count * std::max(1, slot->ctas_per_sm[se])), dim3(256),
                                         args, 0, s);
-    }
-    if (e == cudaSuccess) {
-        noalloc_finalize<<<1, 1, 0, s>>>(base, L, d_out);
-        e = cudaGetLastError();
     }
     if (e != cudaSuccess) {
         cudaGetLastError();

@@ -569,74 +569,6 @@ __global__ void info_init_kernel(const PairDesc* __restrict__ descs, int npairs)
     I->pad[0] = I->pad[1] = 0;
 }
 
-// Robust HD on the device, one warp: the stopping rule of hello.cu:1751-1758
-// (keep dilating while (float)total * p > covered, covered = voxels with
-// distance 1..k) on a per-step histogram.  covered grows with k, so the
-// first k that stops is found 32 steps at a time by a prefix sum and a
-// ballot (a single thread would wait on one load per step).
-__device__ __forceinline__ int robust_k_warp(const unsigned long long* hist, int len, unsigned long long total,
-                                             float p) {
-    const int lane = threadIdx.x & 31;
-    const float tf = (float)total * p;
-    unsigned long long base = 0;
-    for (int k0 = 0; k0 < len; k0 += 32) {
-        const int k = k0 + lane;
-        unsigned long long c = (k > 0 && k < len) ? hist[k] : 0ull;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned long long t = __shfl_up_sync(0xffffffffu, c, o);
-            if (lane >= o) c += t;
-        }
-        const bool stop = k < len && !(tf > (float)(base + c));
-        const unsigned m = __ballot_sync(0xffffffffu, stop);
-        if (m) return k0 + __ffs(m) - 1;
-        base += __shfl_sync(0xffffffffu, c, 31);
-    }
-    return len - 1;
-}
-
-// Decodes each pair's result on the device (one warp per pair), with the
-// rules of the host decoder: statuses, one-sided distances, exact sums,
-// average (one double division), robust HD.
-__global__ void finalize_kernel(const Ctl* __restrict__ ctl, const JobState* __restrict__ states,
-                                const PairDesc* __restrict__ descs, int npairs, float pct, hd_result* out) {
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (i >= npairs) return;  // whole warps leave together
-    const PairDesc& P = descs[i];
-    const PairInfo I = *P.info;
-    const JobState s0 = states[P.job0], s1 = states[P.job0 + 1];
-    hd_result r;
-    memset(&r, 0, sizeof r);
-    r.n_a = I.n_a;
-    r.n_b = I.n_b;
-    r.n_a_not_b = I.n_a - I.n_ab;
-    r.n_b_not_a = I.n_b - I.n_ab;
-    r.iterations = ctl->iters_run;
-    if (I.n_a == 0 && I.n_b == 0) {
-        r.status = HD_OK;
-    } else if (I.n_a == 0 || I.n_b == 0) {
-        r.status = HD_EMPTY_MASK;
-        r.hd = r.hd_ab = r.hd_ba = r.hd_robust = -1;
-        r.avg_hd = __longlong_as_double(0x7ff8000000000000LL);  // quiet NaN
-    } else {
-        int st = ctl->err;
-        if (!st) st = s0.status ? s0.status : s1.status;
-        if (!st && (s0.remaining != 0 || s1.remaining != 0)) st = HD_ERR_ITER_LIMIT;
-        r.status = st;
-        r.hd_ba = s0.hd;  // job 0 dilates A and covers B
-        r.sum_ba = s0.sum;
-        r.hd_ab = s1.hd;
-        r.sum_ab = s1.sum;
-        r.hd = max(r.hd_ab, r.hd_ba);
-        r.avg_hd = (double)(r.sum_ab + r.sum_ba) / (double)(r.n_a + r.n_b);
-        const int kp1 = P.kmax + 1;
-        r.hd_robust = max(robust_k_warp(P.hist[1], kp1, r.n_a_not_b, pct),
-                          robust_k_warp(P.hist[0], kp1, r.n_b_not_a, pct));
-        if (st != HD_OK) r.hd = r.hd_ab = r.hd_ba = r.hd_robust = -1;
-    }
-    if ((threadIdx.x & 31) == 0) out[i] = r;
-}
-
 // Instrumented runs: zero the per-tile stamps and per-step tile counters.
 __global__ void zero_i32_kernel(int32_t* p, long long n) {
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
@@ -698,13 +630,6 @@ cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, 
 cudaError_t launch_info_init(const PairDesc* d_descs, int npairs, cudaStream_t s) {
     if (npairs <= 0) return cudaSuccess;
     info_init_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(d_descs, npairs);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_finalize(const Ctl* ctl, const JobState* states, const PairDesc* d_descs, int npairs, float pct,
-                            hd_result* out, cudaStream_t s) {
-    if (npairs <= 0) return cudaSuccess;
-    finalize_kernel<<<(npairs + 3) / 4, 128, 0, s>>>(ctl, states, d_descs, npairs, pct, out);  // a warp per pair
     return cudaGetLastError();
 }
 

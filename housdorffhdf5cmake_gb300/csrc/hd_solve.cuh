@@ -125,6 +125,72 @@ __device__ __forceinline__ bool grid_step_barrier(Ctl* ctl, unsigned& gen, int g
     return *s_flag != 0;
 }
 
+// Robust HD on the device, one warp: the stopping rule of hello.cu:1751-1758
+// (keep dilating while (float)total * p > covered, covered = voxels with
+// distance 1..k) on a per-step histogram.  covered grows with k, so the
+// first k that stops is found 32 steps at a time by a prefix sum and a
+// ballot (a single thread would wait on one load per step).
+__device__ __forceinline__ int robust_k_warp(const unsigned long long* hist, int len, unsigned long long total,
+                                             float p) {
+    const int lane = threadIdx.x & 31;
+    const float tf = (float)total * p;
+    unsigned long long base = 0;
+    for (int k0 = 0; k0 < len; k0 += 32) {
+        const int k = k0 + lane;
+        unsigned long long c = (k > 0 && k < len) ? hist[k] : 0ull;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long t = __shfl_up_sync(kFull, c, o);
+            if (lane >= o) c += t;
+        }
+        const bool stop = k < len && !(tf > (float)(base + c));
+        const unsigned m = __ballot_sync(kFull, stop);
+        if (m) return k0 + __ffs(m) - 1;
+        base += __shfl_sync(kFull, c, 31);
+    }
+    return len - 1;
+}
+
+// Decodes pair i's result on the device (one warp), with the rules of the
+// host decoder: statuses, one-sided distances, exact sums, average (one
+// double division), robust HD.  Runs after the launch's last grid barrier,
+// when every job's state is final.
+static __device__ __noinline__ void decode_pair_warp(const SolveParams& p, int i, int iters) {
+    const PairDesc& P = p.descs[i];
+    const PairInfo I = *P.info;
+    const JobState s0 = p.states[P.job0], s1 = p.states[P.job0 + 1];
+    hd_result r;
+    memset(&r, 0, sizeof r);
+    r.n_a = I.n_a;
+    r.n_b = I.n_b;
+    r.n_a_not_b = I.n_a - I.n_ab;
+    r.n_b_not_a = I.n_b - I.n_ab;
+    r.iterations = iters;
+    if (I.n_a == 0 && I.n_b == 0) {
+        r.status = HD_OK;
+    } else if (I.n_a == 0 || I.n_b == 0) {
+        r.status = HD_EMPTY_MASK;
+        r.hd = r.hd_ab = r.hd_ba = r.hd_robust = -1;
+        r.avg_hd = __longlong_as_double(0x7ff8000000000000LL);  // quiet NaN
+    } else {
+        int st = ld_relaxed_s32(&p.ctl->err);
+        if (!st) st = s0.status ? s0.status : s1.status;
+        if (!st && (s0.remaining != 0 || s1.remaining != 0)) st = HD_ERR_ITER_LIMIT;
+        r.status = st;
+        r.hd_ba = s0.hd;  // job 0 dilates A and covers B
+        r.sum_ba = s0.sum;
+        r.hd_ab = s1.hd;
+        r.sum_ab = s1.sum;
+        r.hd = max(r.hd_ab, r.hd_ba);
+        r.avg_hd = (double)(r.sum_ab + r.sum_ba) / (double)(r.n_a + r.n_b);
+        const int kp1 = P.kmax + 1;
+        r.hd_robust = max(robust_k_warp(P.hist[1], kp1, r.n_a_not_b, p.pct),
+                          robust_k_warp(P.hist[0], kp1, r.n_b_not_a, p.pct));
+        if (st != HD_OK) r.hd = r.hd_ab = r.hd_ba = r.hd_robust = -1;
+    }
+    if ((threadIdx.x & 31) == 0) p.out[i] = r;
+}
+
 template <int BXW, int BZ, bool SE18>
 __device__ __forceinline__ void brick_step(const SolveParams& p, int jid, unsigned lb, unsigned epoch, int g) {
     constexpr int BY = 32 / BXW;
@@ -380,6 +446,9 @@ __global__ void __launch_bounds__(256, 2) solve_kernel(SolveParams p) {
         ctl->g_end = g;
         ctl->iters_run = it;
     }
+    // results on the device: one warp per pair, after the last barrier
+    if (p.out)
+        for (unsigned i = gw; i < (unsigned)p.npairs; i += nw) decode_pair_warp(p, (int)i, it);
 }
 
 }  // namespace hdk

@@ -572,6 +572,9 @@ __global__ void __launch_bounds__(kTbWarps * 32, kTbMinCtas) solve_tb_kernel(Sol
         ctl->g_end = g;
         ctl->iters_run = it;
     }
+    // results on the device: one warp per pair, after the last barrier
+    if (p.out)
+        for (unsigned i = gw; i < (unsigned)p.npairs; i += nw) decode_pair_warp(p, (int)i, it);
 }
 
 }  // namespace hdk
