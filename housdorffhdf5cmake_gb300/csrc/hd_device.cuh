@@ -76,7 +76,7 @@ constexpr long long kTileWords = 1024;
 // kTbPrefetch planes ahead of the one being computed; a plane stays until
 // its final step has been compared with it, T planes later.  Per warp: the
 // slots (32 rows x (16 B interior + 8 B halo words)) and the brick's
-// uncovered-target rows (BZ planes x 32 rows x 16 B).  3 CTAs of kTbWarps
+// target rows (BZ planes x 32 rows x 16 B).  3 CTAs of kTbWarps
 // warps fit on an SM.
 constexpr int kTbWarps = 4;
 constexpr int kTbPrefetch = 2;

@@ -43,7 +43,7 @@ struct Shape {  // default: the autotuner's choice on the 512x512x256, 512^3 and
     void finish() {
         if (kernel == 2) {
             // kTbWarps warps per CTA, each with a ring of streamed planes and
-            // the brick's uncovered-target rows in shared memory
+            // the brick's target rows in shared memory
             bxw = 4;
             by = 32 - 2 * steps;
             threads = hdk::kTbWarps * 32;

@@ -63,7 +63,7 @@ __device__ __forceinline__ void cp_async_wait_upto(int n) {
 
 // Shared memory of one warp: ring slots of streamed planes (interior words
 // as 16-byte rows, then the two halo words of each row), then the brick's
-// uncovered-target rows.
+// target rows (18-neighbour element: target minus state, updated per level).
 template <int T, int BZ>
 struct TbSmem {
     static constexpr int NP = BZ + 2 * T;  // planes streamed per brick
@@ -374,7 +374,7 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
             // the last level: the domain is a box and every shortest
             // 6-neighbour path between two of its voxels stays inside it, so
             // dilating past its faces for a few levels changes nothing inside
-            // (and the uncovered-target words are zero outside).  The
+            // (and the target words are zero outside).  The
             // 18-neighbour element's paths can leave and re-enter the box: it
             // is clipped at every level, like the reference's border guards.
             if (SE18 || s == T) {
