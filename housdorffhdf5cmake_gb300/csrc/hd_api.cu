@@ -434,7 +434,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         Dd.info = (PairInfo*)(dbase + off_infos) + i;
         Dd.tile0 = pack_tiles;
         Dd.stile0 = setup_tiles;
-        pack_tiles += hdk::tiles_of(hdk::pack_words(P.W, P.H, P.D));
+        pack_tiles += hdk::pack_tiles_of(P.W, P.H, P.D);
         setup_tiles += hdk::setup_tiles_of(P.W, P.H, P.D, setup_mode, bxw, by, bz);
     }
 

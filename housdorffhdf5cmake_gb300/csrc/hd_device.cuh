@@ -65,11 +65,12 @@ struct PairDesc {
     long long stile0;              // first set-up tile of this pair
 };
 
-// Packing and set-up split every pair into tiles of kTileWords words; one
-// launch covers the tiles of all pairs.  Packing tiles cover the packed
-// volume (wxf * H * D words), set-up tiles the domain capacity (rows padded
-// to 4 words: roundup(wxf, 4) * H * D).
+// Packing and set-up split every pair into tiles; one launch covers the
+// tiles of all pairs.  Packing tiles are kPackTileWords words of the packed
+// volume (wxf * H * D words), set-up tiles kTileWords words of the domain
+// capacity (rows padded to 4 words: roundup(wxf, 4) * H * D).
 constexpr long long kTileWords = 1024;
+constexpr long long kPackTileWords = 1024;
 
 // Temporally blocked dilation kernel (hd_solve_tb.cuh): each warp streams
 // the BZ + 2T planes of its brick through a ring of shared-memory slots
@@ -96,6 +97,9 @@ __host__ __device__ __forceinline__ long long domain_cap_words(int W, int H, int
     return (long long)((((W + 31) / 32) + 3) & ~3) * H * D;
 }
 __host__ __device__ __forceinline__ long long tiles_of(long long words) { return (words + kTileWords - 1) / kTileWords; }
+__host__ __device__ __forceinline__ long long pack_tiles_of(int W, int H, int D) {
+    return (pack_words(W, H, D) + kPackTileWords - 1) / kPackTileWords;
+}
 // Bricks of the full volume's brick grid (an upper bound of any domain's).
 __host__ __device__ __forceinline__ long long bricks_max(int W, int H, int D, int bxw, int by, int bz) {
     return (long long)((((W + 31) / 32) + bxw - 1) / bxw) * ((H + by - 1) / by) * ((D + bz - 1) / bz);

@@ -165,7 +165,7 @@ extern "C" hd_status hd_compute_u8_device_noalloc(const uint8_t* d_a, const uint
         e = cudaGetLastError();
     }
     const hdk::PairDesc* desc = (const hdk::PairDesc*)(base + L.desc);
-    const long long ptiles = hdk::tiles_of(hdk::pack_words(W, H, D));
+    const long long ptiles = hdk::pack_tiles_of(W, H, D);
     const long long stiles = hdk::setup_tiles_of(W, H, D, hdk::kSetupOneStep, kBxw, 32 / kBxw, kBz);
     const int cap_ctas = std::max(slot->sm_count * 8, 1);
     if (e == cudaSuccess)  // nonzero bytes are foreground

@@ -161,7 +161,8 @@ __device__ __noinline__ uint32_t chunk_bits_edge(const uint8_t* p, const uint8_t
 
 constexpr int kPackThreads = 256;
 constexpr int kPackGroups = 4;  // words per thread and tile: a warp packs 32 * kPackGroups consecutive words
-static_assert(kTileWords == (kPackThreads / 32) * 32 * kPackGroups, "one tile = one span per warp");
+constexpr int kPackMinCtas = 2;  // resident CTAs per SM (register budget: 65536 / (kPackThreads * kPackMinCtas))
+static_assert(kPackTileWords == (kPackThreads / 32) * 32 * kPackGroups, "one tile = one span per warp");
 
 // Constants of one pair's packing walk (taken when a CTA's run of tiles
 // enters the pair).
@@ -213,7 +214,7 @@ template <bool kEdge, bool kLabel>
 __device__ __forceinline__ void pack_tile(const PairDesc& P, const PackWalk& k, long long tile_in_pair,
                                           PackAcc& acc, int label, uint32_t pat) {
     const int lane = threadIdx.x & 31;
-    const unsigned t0 = (unsigned)(tile_in_pair * kTileWords) + (threadIdx.x >> 5) * (32u * kPackGroups) + lane;
+    const unsigned t0 = (unsigned)(tile_in_pair * kPackTileWords) + (threadIdx.x >> 5) * (32u * kPackGroups) + lane;
     unsigned r = t0 / k.wxf, w = t0 - r * k.wxf;
     unsigned y = r % k.H;
     uint4 c[kPackGroups][2][2];
@@ -318,10 +319,10 @@ __device__ __forceinline__ void pack_tile(const PairDesc& P, const PackWalk& k, 
 // tiles (a run crosses few pairs, so the pair lookup and the accumulator
 // flush are rare).  A tile takes the checked path if it is a pair's first
 // tile or reaches within 48 words of the pair's end: every other word then
-// starts at byte >= kTileWords (each word holds >= 1 byte) and ends >= 48
+// starts at byte >= kPackTileWords (each word holds >= 1 byte) and ends >= 48
 // bytes before the mask's end, so its three chunks lie inside the mask.
 template <bool kLabel>
-__global__ void __launch_bounds__(kPackThreads, 2) pack_kernel(const PairDesc* __restrict__ descs, int npairs,
+__global__ void __launch_bounds__(kPackThreads, kPackMinCtas) pack_kernel(const PairDesc* __restrict__ descs, int npairs,
                                                                long long ntiles, int label) {
     const uint32_t pat = (uint32_t)label * 0x01010101u;
     PackAcc acc;
@@ -342,7 +343,7 @@ __global__ void __launch_bounds__(kPackThreads, 2) pack_kernel(const PairDesc* _
             walk = make_walk(descs[pi]);
         }
         const long long tp = tile - descs[pi].tile0;
-        if (tp >= 1 && (tp + 1) * kTileWords + 48 <= (long long)walk.total)
+        if (tp >= 1 && (tp + 1) * kPackTileWords + 48 <= (long long)walk.total)
             pack_tile<false, kLabel>(descs[pi], walk, tp, acc, label, pat);
         else
             pack_tile<true, kLabel>(descs[pi], walk, tp, acc, label, pat);

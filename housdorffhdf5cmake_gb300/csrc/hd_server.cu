@@ -283,7 +283,7 @@ void tick(hd_server* s) {
         d.epoch = ++s->slot_epoch[r->slot];
         d.tile0 = ptiles;
         d.stile0 = stiles;
-        ptiles += hdk::tiles_of(hdk::pack_words(r->W, r->H, r->D));
+        ptiles += hdk::pack_tiles_of(r->W, r->H, r->D);
         stiles += hdk::setup_tiles_of(r->W, r->H, r->D, setup_mode, s->shape.bxw, s->shape.by, s->shape.bz);
         d.info = (PairInfo*)(rb + r->off_info);
         descs.push_back(d);
