@@ -367,7 +367,10 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     char* hbase = (char*)(async ? ctx->async_stage[slot].ptr : ctx->pinned.ptr);
     const int g0 = ctx->g_next;
     long long pack_tiles = 0, setup_tiles = 0;
-    const int setup_mode = sh.kernel == 1 ? hdk::kSetupOneStep : (n == 1 ? hdk::kSetupBlocked : hdk::kSetupBlockedInPlace);
+    // blocked kernel: a single pair reads the packed masks in place unless
+    // that adds a brick column, a batch always does
+    const int setup_mode =
+        sh.kernel == 1 ? hdk::kSetupOneStep : (n == 1 ? hdk::kSetupBlocked : hdk::kSetupBlockedInPlace);
 
     // ---- asynchronous calls with host masks: copy on the copy stream ------
     const uint8_t* staged[2] = {nullptr, nullptr};
