@@ -98,3 +98,21 @@ def test_cancel(hd, ctx):
         else:
             assert same(r, ctx.compute(a, b, "se6"))
     assert st["cancelled"] >= 1
+
+
+@pytest.mark.parametrize("opts", [{"kernel": 1}, {"kernel": 2, "steps_per_barrier": 4}])
+def test_server_kernels_and_slot_reuse(hd, ctx, opts):
+    """Both dilation kernels under the server (the one-step kernel's queue
+    entries and the blocked kernel's crops), with few slots so that pairs
+    reuse the slots and brick ranges of finished ones."""
+    pairs = _pairs(24, 23, lo=32, hi=112, edge=0.1)
+    plain = [ctx.compute(a, b, "se6") for a, b in pairs]
+    with hd.Context(0, **opts) as c2, hd.Server(c2, tick_iterations=3, max_inflight=3) as srv:
+        ts = []
+        for i, (a, b) in enumerate(pairs):
+            ts.append(srv.submit(a, b))
+            if i % 5 == 0:
+                time.sleep(0.002)
+        res = [srv.wait(t, 60000) for t in ts]
+    for i, (r, p) in enumerate(zip(res, plain)):
+        assert same(r, p), (opts, i, r, p)
