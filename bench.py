@@ -158,16 +158,21 @@ def bench_ours(args):
         phases.append(ctx.last_timings())
         blocking.append(e0.elapsed_time(e1))
     phases = phases[-2:]
-    # warm-up of the enqueue-only entry used in the timed region
+    # warm-up of the enqueue-only entries used in the timed regions (the
+    # first pipelined call sets up the split SMs and the second workspace)
     outs = torch.empty((args.steps, hd.RESULT_BYTES), dtype=torch.uint8, device=dev)
     for w in range(max(args.warmup, 6)):
         x, y = pairs[w % 2]
         ctx.compute_async(x, y, "se6", out=outs[w % args.steps])
+        ctx.compute_pipelined(x, y, "se6", out=outs[(w + 1) % args.steps])
+    ctx.flush()
     torch.cuda.synchronize()
 
     # ---- device-resident timed region ---------------------------------------
-    # K pairs enqueued back to back through hd_compute_u8_device_async (each
-    # result decoded on the device into its own slot), one synchronisation
+    # K pairs enqueued back to back through hd_compute_u8_device_pipelined
+    # (each result decoded on the device into its own slot; a pair's packing
+    # and set-up run beside the previous pair's dilation), one flush, one
+    # synchronisation
     clocks = ClockSampler(local)
     with clocks:
         if dist:
@@ -178,7 +183,8 @@ def bench_ours(args):
         e0.record(stream)
         for k in range(args.steps):
             x, y = pairs[k % 2]
-            ctx.compute_async(x, y, "se6", out=outs[k])
+            ctx.compute_pipelined(x, y, "se6", out=outs[k])
+        ctx.flush()
         e1.record(stream)
         e1.synchronize()
         torch.cuda.synchronize()
@@ -189,6 +195,20 @@ def bench_ours(args):
     host_outs = outs.cpu()
     for k in range(args.steps):
         assert hd.result_from_bytes(host_outs[k]) == refs[k % 2], f"step {k}: result differs"
+    # the same K pairs through hd_compute_u8_device_async (each pair waits for
+    # the previous one to finish on the stream)
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    for k in range(args.steps):
+        x, y = pairs[k % 2]
+        ctx.compute_async(x, y, "se6", out=outs[k])
+    s1.record(stream)
+    s1.synchronize()
+    serial_ms = s0.elapsed_time(s1) / args.steps
+    host_outs = outs.cpu()
+    for k in range(args.steps):
+        assert hd.result_from_bytes(host_outs[k]) == refs[k % 2], f"async step {k}: result differs"
     clk = clocks.summary()
     step_ms = sum(times) / len(times)
     if dist:
@@ -317,6 +337,10 @@ def bench_ours(args):
                 "blocking_path": "hd_compute_u8, one call per pair, masks read in place over the host link",
                 "staged_copy_ms_per_step": round(staged_ms, 4)},
         "gpu_launches": 3 * args.steps,  # per pair: pack, set-up, persistent dilation (decodes the result too)
+        "value_path": "hd_compute_u8_device_pipelined x K, hd_pipeline_flush: pair k+1's packing and set-up on "
+                      "a few SMs beside pair k's dilation on the rest (green contexts)",
+        "async_serial": {"path": "hd_compute_u8_device_async x K (each pair after the previous one)",
+                         "ms_per_step": round(serial_ms, 4), "pairs_per_s": round(1000.0 / serial_ms, 1)},
         "blocking_call": {"path": "hd_compute_u8_device (returns the result to the host each call)",
                           "ms_per_step": round(statistics.mean(blocking), 4),
                           "pairs_per_s": round(1000.0 / statistics.mean(blocking), 1)},

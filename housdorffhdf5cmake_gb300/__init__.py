@@ -285,6 +285,33 @@ class Context:
         _check(code, self._h, allow_empty=False)
         return out
 
+    def compute_pipelined(self, a, b, metric="se6", out=None, stream=None):
+        """Enqueues one pair of CUDA masks through hd_compute_u8_device_pipelined
+        on `stream` (default: torch's current stream) and returns at once.
+        The result lands in `out` (a CUDA uint8 tensor of RESULT_BYTES bytes,
+        allocated if None) once the stream reaches a later flush(); meanwhile
+        the next pair's packing may run beside this pair's dilation.  Calls
+        on one context must stay on one stream."""
+        import torch
+        A, B = _Buf(a), _Buf(b)
+        if (A.W, A.H, A.D) != (B.W, B.H, B.D):
+            raise ValueError("mask shapes differ")
+        if not (A.on_device and B.on_device):
+            raise ValueError("compute_pipelined() takes CUDA masks")
+        if out is None:
+            out = torch.empty(RESULT_BYTES, dtype=torch.uint8, device=A.obj.device)
+        s = _current_stream_ptr() if stream is None else stream
+        code = N.load().hd_compute_u8_device_pipelined(self._h, A.ptr, B.ptr, A.W, A.H, A.D, metric_code(metric),
+                                                       ctypes.c_void_p(s), ctypes.c_void_p(out.data_ptr()))
+        _check(code, self._h, allow_empty=False)
+        return out
+
+    def flush(self, stream=None):
+        """hd_pipeline_flush: `stream` (default: torch's current stream)
+        waits for every pipelined call so far."""
+        s = _current_stream_ptr() if stream is None else stream
+        _check(N.load().hd_pipeline_flush(self._h, ctypes.c_void_p(s)), self._h)
+
     # -- batches --------------------------------------------------------------
     def batch(self, pairs: Sequence, metric="se6") -> list:
         """One hd_batch_compute over [(a, b), ...] (host or CUDA masks).

@@ -30,7 +30,8 @@ HD_SE18_FORBENCH = 1
 EXPORTS = (
     "hd_options_init", "hd_status_string", "hd_version", "hd_context_create", "hd_context_destroy",
     "hd_context_last_error", "hd_context_last_timings", "hd_compute_u8", "hd_compute_u8_device",
-    "hd_compute_u8_device_async", "hd_compute_u8_async", "hd_batch_compute",
+    "hd_compute_u8_device_async", "hd_compute_u8_async", "hd_compute_u8_device_pipelined", "hd_pipeline_flush",
+    "hd_batch_compute",
     "hd_profile_u8_device", "hd_distance_map_device", "hd_autotune", "hd_server_options_init",
     "hd_server_create", "hd_server_submit", "hd_server_poll", "hd_server_wait", "hd_server_cancel",
     "hd_server_get_stats", "hd_server_destroy", "hd_compute_u8_device_noalloc", "hd_load_hdf5_bool", "hd_free",
@@ -169,6 +170,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             "hd_compute_u8_device": (st, [vp, vp, vp, i32, i32, i32, st, vp, res_p]),
             "hd_compute_u8_device_async": (st, [vp, vp, vp, i32, i32, i32, st, vp, vp]),
             "hd_compute_u8_async": (st, [vp, vp, vp, i32, i32, i32, st, vp, vp]),
+            "hd_compute_u8_device_pipelined": (st, [vp, vp, vp, i32, i32, i32, st, vp, vp]),
+            "hd_pipeline_flush": (st, [vp, vp]),
             "hd_batch_compute": (st, [vp, ctypes.POINTER(HdPairDesc), i32, res_p]),
             "hd_profile_u8_device": (st, [vp, vp, vp, i32, i32, i32, st, res_p, u64p, u64p, i32, u64p]),
             "hd_distance_map_device": (st, [vp, vp, vp, i32, i32, i32, st, vp, vp, res_p]),

@@ -7,12 +7,14 @@
 // step on the device, and one read-back of a few hundred bytes.  No host
 // round trip per step (the reference does a blocking symbol read per step at
 // :167), no cudaDeviceReset, no exit.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "hd/hd.h"
@@ -166,6 +168,102 @@ int occupancy_of(hd_context* ctx, const void* fn, int threads, int smem) {
     n = std::max(1, n);
     ctx->occupancy[fn] = n;
     return n;
+}
+
+namespace {
+
+// Driver entry points of the green-context API, through the runtime (no
+// link against the driver library).
+template <class F>
+F driver_fn(const char* name, int version) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion(name, &fn, version, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return reinterpret_cast<F>(fn);
+}
+
+using GreenDestroyFn = CUresult (*)(CUgreenCtx);
+
+}  // namespace
+
+// SMs given to packing and set-up on the split path (a multiple of the
+// partition granularity, 8 SMs on GB300); the rest dilate.  Measured on the
+// 512x512x256 pairs: 24 / 32 / 48 / 64 SMs -> 155 / 127 / 112 / 121 us per
+// pair (142 us unsplit).
+constexpr unsigned kSplitPrepSms = 48;
+
+// HD_SPLIT_SMS in the environment overrides it: 0 = no split (profilers
+// that cannot follow kernels into green contexts), else the SMs to give to
+// packing and set-up.
+bool split_ready(hd_context* ctx) {
+    hd_context::Split& sp = ctx->split;
+    if (sp.state) return sp.state > 0;
+    sp.state = -1;
+    unsigned prep_want = kSplitPrepSms;
+    if (const char* env = std::getenv("HD_SPLIT_SMS")) {
+        const long v = std::strtol(env, nullptr, 10);
+        if (v <= 0) return false;
+        prep_want = (unsigned)v;
+    }
+    auto get_dev = driver_fn<CUresult (*)(CUdevice*, int)>("cuDeviceGet", 2000);
+    auto get_res = driver_fn<CUresult (*)(CUdevice, CUdevResource*, CUdevResourceType)>("cuDeviceGetDevResource", 12040);
+    auto split = driver_fn<CUresult (*)(CUdevResource*, unsigned*, const CUdevResource*, CUdevResource*, unsigned,
+                                        unsigned)>("cuDevSmResourceSplitByCount", 12040);
+    auto make_desc = driver_fn<CUresult (*)(CUdevResourceDesc*, CUdevResource*, unsigned)>("cuDevResourceGenerateDesc",
+                                                                                         12040);
+    auto create = driver_fn<CUresult (*)(CUgreenCtx*, CUdevResourceDesc, CUdevice, unsigned)>("cuGreenCtxCreate", 12040);
+    auto stream = driver_fn<CUresult (*)(CUstream*, CUgreenCtx, unsigned, int)>("cuGreenCtxStreamCreate", 12050);
+    if (!get_dev || !get_res || !split || !make_desc || !create || !stream) return false;
+    CUdevice dev;
+    CUdevResource all{}, prep{}, rest{};
+    unsigned groups = 1;
+    if (get_dev(&dev, ctx->device) != CUDA_SUCCESS || get_res(dev, &all, CU_DEV_RESOURCE_TYPE_SM) != CUDA_SUCCESS)
+        return false;
+    if (all.sm.smCount < prep_want + 64) return false;  // too few SMs to give some away
+    if (split(&prep, &groups, &all, &rest, 0, prep_want) != CUDA_SUCCESS || groups != 1) return false;
+    CUdevResourceDesc d[2];
+    CUgreenCtx g[2] = {nullptr, nullptr};
+    CUstream st[2] = {nullptr, nullptr};
+    bool ok = make_desc(&d[0], &rest, 1) == CUDA_SUCCESS && make_desc(&d[1], &prep, 1) == CUDA_SUCCESS;
+    for (int i = 0; i < 2 && ok; ++i) ok = create(&g[i], d[i], dev, CU_GREEN_CTX_DEFAULT_STREAM) == CUDA_SUCCESS;
+    for (int i = 0; i < 2 && ok; ++i) ok = stream(&st[i], g[i], CU_STREAM_NON_BLOCKING, 0) == CUDA_SUCCESS;
+    cudaError_t e = ok ? cudaSuccess : cudaErrorUnknown;
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sp.caller, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sp.prep_done, cudaEventDisableTiming);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&sp.ws_free[i], cudaEventDisableTiming);
+    sp.green[0] = g[0];
+    sp.green[1] = g[1];
+    sp.solve = (cudaStream_t)st[0];
+    sp.prep = (cudaStream_t)st[1];
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        split_release(ctx);
+        sp.state = -1;
+        return false;
+    }
+    sp.solve_sms = (int)rest.sm.smCount;
+    sp.prep_sms = (int)prep.sm.smCount;
+    sp.state = 1;
+    return true;
+}
+
+void split_release(hd_context* ctx) {
+    hd_context::Split& sp = ctx->split;
+    for (cudaStream_t s : {sp.solve, sp.prep})
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    for (cudaEvent_t ev : {sp.caller, sp.prep_done, sp.ws_free[0], sp.ws_free[1]})
+        if (ev) cudaEventDestroy(ev);
+    auto destroy = driver_fn<GreenDestroyFn>("cuGreenCtxDestroy", 12040);
+    for (void* g : sp.green)
+        if (g && destroy) destroy((CUgreenCtx)g);
+    sp = hd_context::Split{};
 }
 
 namespace {
@@ -330,18 +428,49 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     const size_t total_bytes = cur;
     const size_t pinned_bytes = upload_bytes + sizeof(uint64_t) * (hist_words + (stats ? hist_words : 0));
 
-    cudaError_t e = ctx->arena.ensure(total_bytes);
+    // Pipelined single pairs of up to 2^26 voxels run on split SMs: their
+    // dilation is latency-bound and fits fewer SMs, so the next pair's
+    // packing and set-up (bandwidth-bound) run beside it, on their own SMs
+    // and workspace.  Streams: sq (uploads, packing, set-up) and sv (the
+    // dilation), both the caller's stream otherwise.  The caller's stream
+    // waits for the dilations only at a flush (or the next other call).
+    const bool async = ro.async_out != nullptr;
+    const bool split = async && ro.pipelined && n == 1 && sh.kernel == 2 &&
+                       (double)pairs[0].W * pairs[0].H * pairs[0].D <= (double)(1 << 26) && split_ready(ctx);
+    if (!split && ctx->split.pending) {  // every other call follows the pipelined ones
+        cudaError_t e0 = cudaStreamWaitEvent(s, ctx->split.ws_free[ctx->split.last], 0);
+        if (e0 != cudaSuccess) return cuda_fail(ctx, e0, "pipeline flush");
+        ctx->split.pending = false;
+    }
+    const int ws = split ? ctx->split.next : 0;
+    if (split) ctx->split.next ^= 1;
+    DeviceArena& arena = ws ? ctx->arena2 : ctx->arena;
+    cudaStream_t sq = split ? ctx->split.prep : s, sv = split ? ctx->split.solve : s;
+    const int prep_sms = split ? ctx->split.prep_sms : ctx->sm_count;
+
+    cudaError_t e = arena.ensure(total_bytes);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "device workspace");
+    if (split) {
+        // the packing waits for the caller's earlier work and for the
+        // dilation that last used this workspace
+        e = cudaEventRecord(ctx->split.caller, s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(sq, ctx->split.caller, 0);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(sq, ctx->split.ws_free[ws], 0);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "split streams");
+    }
     if (total_bricks > ctx->stamp_slots || ctx->g_next > (1 << 30)) {
         const size_t want = std::max<size_t>(total_bricks, ctx->stamp_slots);
         e = ctx->stamps.ensure(sizeof(int32_t) * want);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "brick stamps");
-        e = cudaMemsetAsync(ctx->stamps.ptr, 0, sizeof(int32_t) * want, s);
+        // the stamps belong to every dilation of the context: the reset
+        // follows the last one (split path: the other workspace's) and
+        // precedes this call's
+        if (split) e = cudaStreamWaitEvent(sq, ctx->split.ws_free[ws ^ 1], 0);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->stamps.ptr, 0, sizeof(int32_t) * want, sq);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "stamp reset");
         ctx->stamp_slots = want;
         ctx->g_next = 1;
     }
-    const bool async = ro.async_out != nullptr;
     int slot = -1;
     if (async) {
         // first asynchronous call: every staging buffer and event at once
@@ -363,7 +492,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "pinned staging");
 
-    char* dbase = (char*)ctx->arena.ptr;
+    char* dbase = (char*)arena.ptr;
     char* hbase = (char*)(async ? ctx->async_stage[slot].ptr : ctx->pinned.ptr);
     const int g0 = ctx->g_next;
     long long pack_tiles = 0, setup_tiles = 0;
@@ -398,7 +527,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         if (e == cudaSuccess && pairs[0].host_b)
             e = cudaMemcpyAsync(sb, pairs[0].host_b, nb, cudaMemcpyHostToDevice, ctx->copy_stream);
         if (e == cudaSuccess) e = cudaEventRecord(ctx->mask_ready[mb], ctx->copy_stream);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ctx->mask_ready[mb], 0);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(sq, ctx->mask_ready[mb], 0);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "mask copy");
         staged[0] = pairs[0].host_a ? sa : nullptr;
         staged[1] = pairs[0].host_b ? sb : nullptr;
@@ -442,17 +571,17 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     }
 
     // ---- uploads ----------------------------------------------------------
-    e = cudaMemcpyAsync(dbase, hbase, upload_bytes, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess && async) e = cudaEventRecord(ctx->async_done[slot], s);
+    e = cudaMemcpyAsync(dbase, hbase, upload_bytes, cudaMemcpyHostToDevice, sq);
+    if (e == cudaSuccess && async) e = cudaEventRecord(ctx->async_done[slot], sq);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "descriptor upload");
     for (int i = 0; i < n && mb < 0; ++i) {
         const size_t nb = (size_t)pairs[i].W * pairs[i].H * pairs[i].D;
         if (pairs[i].host_a) {
-            e = cudaMemcpyAsync(dbase + plan[i].off_in_a, pairs[i].host_a, nb, cudaMemcpyHostToDevice, s);
+            e = cudaMemcpyAsync(dbase + plan[i].off_in_a, pairs[i].host_a, nb, cudaMemcpyHostToDevice, sq);
             if (e != cudaSuccess) return cuda_fail(ctx, e, "mask upload");
         }
         if (pairs[i].host_b) {
-            e = cudaMemcpyAsync(dbase + plan[i].off_in_b, pairs[i].host_b, nb, cudaMemcpyHostToDevice, s);
+            e = cudaMemcpyAsync(dbase + plan[i].off_in_b, pairs[i].host_b, nb, cudaMemcpyHostToDevice, sq);
             if (e != cudaSuccess) return cuda_fail(ctx, e, "mask upload");
         }
     }
@@ -469,13 +598,13 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
 
     // ---- pack, set-up -----------------------------------------------------
     // one CTA per tile up to 8 per SM, then striding
-    const int grid_pack = (int)std::min<long long>(std::max(ctx->sm_count * 8, 1), pack_tiles);
-    const int grid_setup = (int)std::min<long long>(std::max(ctx->sm_count * 8, 1), setup_tiles);
+    const int grid_pack = (int)std::min<long long>(std::max(prep_sms * 8, 1), pack_tiles);
+    const int grid_setup = (int)std::min<long long>(std::max(prep_sms * 8, 1), setup_tiles);
     const PairDesc* ddesc = (const PairDesc*)(dbase + off_descs);
     const bool timing = ctx->opt.record_timings != 0 && ctx->ev[0] != nullptr && !async;
     if (timing) cudaEventRecord(ctx->ev[0], s);
-    e = hdk::launch_pack(ddesc, n, pack_tiles, grid_pack, ctx->opt.label, s);
-    if (e == cudaSuccess && mb >= 0) e = cudaEventRecord(ctx->mask_free[mb], s);  // staging buffer read
+    e = hdk::launch_pack(ddesc, n, pack_tiles, grid_pack, ctx->opt.label, split ? prep_sms : 0, sq);
+    if (e == cudaSuccess && mb >= 0) e = cudaEventRecord(ctx->mask_free[mb], sq);  // staging buffer read
     if (e != cudaSuccess) return cuda_fail(ctx, e, "pack launch");
     Ctl* dctl = (Ctl*)(dbase + off_ctl);
     Job* djobs = (Job*)(dbase + off_jobs);
@@ -485,7 +614,11 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
                                  (unsigned long long*)(dbase + off_q[2])};
     if (timing) cudaEventRecord(ctx->ev[1], s);
     e = hdk::launch_setup(ddesc, n, setup_tiles, grid_setup, djobs, dstates, dq[g0 % 3], dctl, g0, bxw, by, bz,
-                          setup_mode, s);
+                          setup_mode, sq);
+    if (e == cudaSuccess && split) {
+        e = cudaEventRecord(ctx->split.prep_done, sq);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(sv, ctx->split.prep_done, 0);
+    }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "setup launch");
     if (ro.map_a || ro.map_b) {
         e = hdk::launch_map_init(ddesc, ro.map_a, ro.map_b,
@@ -512,7 +645,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     const int occ = occupancy_of(ctx, solve_fn, sh.threads, sh.smem);
     if (occ <= 0) return set_error(ctx, HD_ERR_CUDA, "dilation kernel cannot be made resident");
     const int per_sm = cps > 0 ? std::min(cps, occ) : occ;
-    dim3 grid(ctx->sm_count * per_sm), block(sh.threads);
+    dim3 grid((split ? ctx->split.solve_sms : ctx->sm_count) * per_sm), block(sh.threads);
     const float pct = (ctx->opt.percentile > 0.f && ctx->opt.percentile <= 1.f) ? ctx->opt.percentile : 0.95f;
     if (async) {  // the launch decodes the results on the device
         sp.descs = ddesc;
@@ -522,7 +655,12 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     }
     void* args[] = {&sp};
     if (timing) cudaEventRecord(ctx->ev[2], s);
-    e = cudaLaunchCooperativeKernel(solve_fn, grid, block, args, (size_t)sh.smem, s);
+    e = cudaLaunchCooperativeKernel(solve_fn, grid, block, args, (size_t)sh.smem, sv);
+    if (e == cudaSuccess && split) {
+        e = cudaEventRecord(ctx->split.ws_free[ws], sv);
+        ctx->split.pending = true;
+        ctx->split.last = ws;
+    }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "dilation launch");
     if (timing) cudaEventRecord(ctx->ev[3], s);
     if (async) {
@@ -696,7 +834,9 @@ hd_status hd_context_destroy(hd_context* ctx) {
         std::lock_guard<std::mutex> lk(ctx->mu);
         DeviceGuard g(ctx->device);
         if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+        split_release(ctx);
         ctx->arena.release();
+        ctx->arena2.release();
         ctx->stamps.release();
         ctx->pinned.release();
         for (int i = 0; i < hd_context::kAsyncSlots; ++i) {
@@ -790,6 +930,38 @@ hd_status hd_compute_u8_device_async(hd_context* ctx, const uint8_t* d_a, const 
     ro.se = se;
     ro.async_out = d_out;
     return run_pairs(ctx, &p, 1, stream ? (cudaStream_t)stream : ctx->stream, ro, nullptr);
+}
+
+hd_status hd_compute_u8_device_pipelined(hd_context* ctx, const uint8_t* d_a, const uint8_t* d_b, int32_t W,
+                                         int32_t H, int32_t D, hd_metric metric, void* stream, hd_result* d_out) {
+    if (!ctx || !d_a || !d_b || !d_out) return HD_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    int se = 0;
+    hd_status st = metric_to_se(ctx, metric, &se);
+    if (st == HD_OK) st = check_dims(ctx, W, H, D);
+    if (st != HD_OK) return st;
+    DeviceGuard g(ctx->device);
+    if (!g.ok) return set_error(ctx, HD_ERR_CUDA, "cannot select device %d", ctx->device);
+    PairIn p{d_a, d_b, W, H, D, nullptr, nullptr};
+    RunOpts ro;
+    ro.se = se;
+    ro.async_out = d_out;
+    ro.pipelined = true;
+    return run_pairs(ctx, &p, 1, stream ? (cudaStream_t)stream : ctx->stream, ro, nullptr);
+}
+
+hd_status hd_pipeline_flush(hd_context* ctx, void* stream) {
+    if (!ctx) return HD_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (!ctx->split.pending) return HD_OK;
+    DeviceGuard g(ctx->device);
+    if (!g.ok) return set_error(ctx, HD_ERR_CUDA, "cannot select device %d", ctx->device);
+    // the dilations run in order on one stream: the latest covers them all
+    cudaError_t e = cudaStreamWaitEvent(stream ? (cudaStream_t)stream : ctx->stream,
+                                        ctx->split.ws_free[ctx->split.last], 0);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "pipeline flush");
+    ctx->split.pending = false;
+    return HD_OK;
 }
 
 hd_status hd_compute_u8_async(hd_context* ctx, const uint8_t* a, const uint8_t* b, int32_t W, int32_t H, int32_t D,

@@ -114,6 +114,21 @@ struct hd_context {
     hdh::DeviceArena mask_stage[2];
     cudaEvent_t mask_ready[2] = {nullptr, nullptr}, mask_free[2] = {nullptr, nullptr};
     int mask_next = 0;
+    // asynchronous single pairs on split SMs (two green contexts): pair k + 1
+    // is packed and set up on a few SMs while pair k dilates on the rest;
+    // the two alternate between two workspaces
+    struct Split {
+        int state = 0;                      // 0 not tried, 1 ready, -1 unavailable
+        void* green[2] = {nullptr, nullptr};  // CUgreenCtx: [0] dilation, [1] packing and set-up
+        cudaStream_t solve = nullptr, prep = nullptr;
+        int solve_sms = 0, prep_sms = 0;
+        cudaEvent_t caller = nullptr, prep_done = nullptr;
+        cudaEvent_t ws_free[2] = {nullptr, nullptr};  // the dilation that last used workspace i
+        int next = 0;
+        bool pending = false;  // a dilation the caller's stream has not waited for yet
+        int last = 0;          // the workspace of the latest dilation
+    } split;
+    hdh::DeviceArena arena2;  // the split path's second workspace
 };
 
 namespace hdh {
@@ -139,6 +154,7 @@ struct RunOpts {
     bool force_shape = false;  // use `shape` as given (autotuner)
     Shape shape;
     hd_result* async_out = nullptr;  // device memory: enqueue only, results decoded on the device
+    bool pipelined = false;          // with async_out: the result may complete after a later flush
 };
 
 hd_status set_error(hd_context* ctx, hd_status st, const char* fmt, ...);
@@ -173,6 +189,11 @@ hd_status decode_result(const hdk::PairInfo& I, const hdk::JobState& s0, const h
 // and `smem` bytes of dynamic shared memory (cached per context; raises the
 // kernel's dynamic shared memory limit first when needed).
 int occupancy_of(hd_context* ctx, const void* fn, int threads, int smem);
+
+// Split SMs for asynchronous single pairs (hd_context::Split): set up on
+// first use; false when green contexts are unavailable.  split_release ends it.
+bool split_ready(hd_context* ctx);
+void split_release(hd_context* ctx);
 
 // Percentile HD of one direction with the reference's float stopping rule.
 int robust_k(const uint64_t* hist, int len, uint64_t total, float p);

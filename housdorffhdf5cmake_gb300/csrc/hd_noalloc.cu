@@ -169,7 +169,7 @@ extern "C" hd_status hd_compute_u8_device_noalloc(const uint8_t* d_a, const uint
     const long long stiles = hdk::setup_tiles_of(W, H, D, hdk::kSetupOneStep, kBxw, 32 / kBxw, kBz);
     const int cap_ctas = std::max(slot->sm_count * 8, 1);
     if (e == cudaSuccess)  // nonzero bytes are foreground
-        e = hdk::launch_pack(desc, 1, ptiles, (int)std::min<long long>(cap_ctas, ptiles), 0, s);
+        e = hdk::launch_pack(desc, 1, ptiles, (int)std::min<long long>(cap_ctas, ptiles), 0, 0, s);
     hdk::Job* jobs = (hdk::Job*)(base + L.jobs);
     hdk::JobState* states = (hdk::JobState*)(base + L.states);
     hdk::Ctl* ctl = (hdk::Ctl*)(base + L.ctl);

@@ -595,9 +595,11 @@ __global__ void map_init_kernel(const PairDesc* __restrict__ descs, int32_t* map
 // ---- launch wrappers (called from the host orchestration) -----------------
 namespace hdk {
 
-cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, int grid, int label, cudaStream_t s) {
+cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, int grid, int label, int sms,
+                        cudaStream_t s) {
     // one wave of resident CTAs (per device and variant, from the occupancy calculator)
     static int resident[2][64] = {{0}};
+    static int per_sm_of[2][64] = {{0}};
     const int v = label ? 1 : 0;
     const void* fn = label ? reinterpret_cast<const void*>(&pack_kernel<true>)
                            : reinterpret_cast<const void*>(&pack_kernel<false>);
@@ -605,13 +607,14 @@ cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, i
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 64 && resident[v][dev] == 0) {
-        int per_sm = 0, sms = 0;
+        int per_sm = 0, sms_dev = 0;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPackThreads, 0);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms_dev, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return e;
-        resident[v][dev] = std::max(1, per_sm) * std::max(1, sms);
+        resident[v][dev] = std::max(1, per_sm) * std::max(1, sms_dev);
+        per_sm_of[v][dev] = std::max(1, per_sm);
     }
-    if (dev < 64) grid = resident[v][dev];
+    if (dev < 64) grid = sms > 0 ? per_sm_of[v][dev] * sms : resident[v][dev];
     if (grid > ntiles) grid = (int)ntiles;
     if (grid < 1) grid = 1;
     if (label) pack_kernel<true><<<grid, kPackThreads, 0, s>>>(d_descs, npairs, ntiles, label);

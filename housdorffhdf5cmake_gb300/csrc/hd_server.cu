@@ -298,7 +298,7 @@ void tick(hd_server* s) {
         const int cap_ctas = std::max(s->ctx->sm_count * 8, 1);
         if (e == cudaSuccess)
             e = hdk::launch_pack(s->d_descs, (int)admitted.size(), ptiles, (int)std::min<long long>(cap_ctas, ptiles),
-                                 s->ctx->opt.label, st);
+                                 s->ctx->opt.label, 0, st);
         if (e == cudaSuccess)
             e = hdk::launch_setup(s->d_descs, (int)admitted.size(), stiles, (int)std::min<long long>(cap_ctas, stiles),
                                   s->d_jobs, s->d_states,

@@ -169,6 +169,23 @@ typedef struct hd_pair_desc {
 hd_status hd_compute_u8_device_async(hd_context* ctx, const uint8_t* d_a, const uint8_t* d_b, int32_t W,
                                      int32_t H, int32_t D, hd_metric metric, void* stream, hd_result* d_out);
 
+/* Pipelined form of hd_compute_u8_device_async; no counterpart in the
+ * reference.  The masks must be ready in `stream` order when the call is
+ * made, as there.  The result of a call is complete once `stream` reaches a
+ * later hd_pipeline_flush(ctx, stream) (any other call on the context also
+ * waits for it first), so a pair's packing and set-up may run while the
+ * previous pair still dilates: single pairs of up to 2^26 voxels on a GPU
+ * whose SMs can be split (green contexts) run their packing and set-up on a
+ * few SMs and their dilation on the rest, with two workspaces in turn.
+ * Otherwise the call behaves like hd_compute_u8_device_async. */
+hd_status hd_compute_u8_device_pipelined(hd_context* ctx, const uint8_t* d_a, const uint8_t* d_b, int32_t W,
+                                         int32_t H, int32_t D, hd_metric metric, void* stream, hd_result* d_out);
+
+/* Makes `stream` (NULL = the context's stream) wait for every pipelined call
+ * made so far on the context; their results are complete once it gets
+ * there. */
+hd_status hd_pipeline_flush(hd_context* ctx, void* stream);
+
 /* Asynchronous form of hd_compute_u8 (HOST masks); no counterpart in the
  * reference.  The masks are copied by DMA on the context's copy stream into
  * one of two device staging buffers, so the copy of one pair overlaps the

@@ -370,6 +370,47 @@ def test_async_entry_matches_blocking_entry(hd, ctx):
                                         None) == hd.HD_ERR_BAD_ARG
 
 
+def test_pipelined_entry_matches_blocking_entry(hd, ctx):
+    """hd_compute_u8_device_pipelined: back-to-back pairs (two workspaces in
+    turn on split SMs; the 512x512x257 pair is above the split's size limit
+    and runs like the asynchronous entry), a blocking call in the middle
+    (which waits for the pipelined ones first), results complete after
+    flush(), equal field by field to hd_compute_u8_device."""
+    from housdorffhdf5cmake_gb300 import _native as N
+    rng = np.random.default_rng(8)
+    cases = []
+    for i, shape in enumerate([(24, 40, 56), (64, 96, 130), (9, 17, 33), (80, 120, 200)]):
+        a, b = random_pair(rng, shape, p_a=0.02, p_b=0.01)
+        cases.append((cuda(a), cuda(b), "se6" if i % 2 == 0 else "se18"))
+    for seed, d in ((31, 256), (32, 257)):
+        a, b = synth.pair_shifted_union(seed, (d, 512, 512), "cuda", rmin=10, rmax=60, max_shift=12)
+        cases.append((a, b, "se6"))
+    z = torch.zeros((12, 20, 36), dtype=torch.uint8, device="cuda")
+    cases.append((z, z.clone(), "se6"))
+    want = [ctx.compute(a, b, m) for a, b, m in cases]
+    with hd.Context(0) as c:
+        outs = []
+        for rep in range(2):
+            for i, (a, b, m) in enumerate(cases):
+                outs.append(c.compute_pipelined(a, b, m))
+                if rep == 0 and i == 3:  # another call in between waits for the pipelined ones
+                    mid = c.compute(*cases[0][:2], cases[0][2])
+        c.flush()
+        torch.cuda.current_stream().synchronize()
+        got = [hd.result_from_bytes(o.cpu()) for o in outs]
+    for k in want[0]:
+        assert mid[k] == want[0][k] or (k == "avg_hd" and mid[k] != mid[k])
+    for i, g in enumerate(got):
+        w = want[i % len(cases)]
+        for k in w:
+            if k == "avg_hd" and w[k] != w[k]:
+                assert g[k] != g[k], (i, k)
+            elif k != "iterations":
+                assert g[k] == w[k], (i, k, g, w)
+    L = N.load()
+    assert L.hd_pipeline_flush(None, None) == hd.HD_ERR_BAD_ARG
+
+
 def test_label_selection(hd, ctx, oracle):
     """label option (the reference's numberToLookFor): a voxel is foreground
     iff its byte equals the label; results equal the binary path on the
