@@ -103,7 +103,7 @@ def _result_dicts(res, n):
     """hd_result array -> list of dicts, column-wise through numpy."""
     arr = np.frombuffer(res, dtype=_RESULT_DTYPE, count=n)
     cols = [arr[f].tolist() for f in _RESULT_FIELDS]
-    return [dict(zip(_RESULT_FIELDS, vals)) for vals in zip(*cols)]
+    return list(map(dict, map(zip, [_RESULT_FIELDS] * n, zip(*cols))))
 
 
 class _Buf:
@@ -203,6 +203,7 @@ class Context:
             raise HDError(code, f"hd_context_create(device={device})")
         self._h = h
         self.device = device
+        self._unflushed = []  # outputs of pipelined calls not yet flushed
 
     # -- lifetime -----------------------------------------------------------
     def close(self):
@@ -290,8 +291,12 @@ class Context:
         on `stream` (default: torch's current stream) and returns at once.
         The result lands in `out` (a CUDA uint8 tensor of RESULT_BYTES bytes,
         allocated if None) once the stream reaches a later flush(); meanwhile
-        the next pair's packing may run beside this pair's dilation.  Calls
-        on one context must stay on one stream."""
+        the next pair's packing may run beside this pair's dilation.  The
+        stream waits for the packing's reads of the masks, so they may be
+        reused or freed in stream order after the call; `out` is written by
+        the dilation, which the stream waits for only at flush(), so the
+        context keeps a reference to it until then.  Calls on one context
+        must stay on one stream."""
         import torch
         A, B = _Buf(a), _Buf(b)
         if (A.W, A.H, A.D) != (B.W, B.H, B.D):
@@ -304,6 +309,7 @@ class Context:
         code = N.load().hd_compute_u8_device_pipelined(self._h, A.ptr, B.ptr, A.W, A.H, A.D, metric_code(metric),
                                                        ctypes.c_void_p(s), ctypes.c_void_p(out.data_ptr()))
         _check(code, self._h, allow_empty=False)
+        self._unflushed.append(out)
         return out
 
     def flush(self, stream=None):
@@ -311,6 +317,7 @@ class Context:
         waits for every pipelined call so far."""
         s = _current_stream_ptr() if stream is None else stream
         _check(N.load().hd_pipeline_flush(self._h, ctypes.c_void_p(s)), self._h)
+        self._unflushed = []
 
     # -- batches --------------------------------------------------------------
     def batch(self, pairs: Sequence, metric="se6") -> list:
@@ -322,15 +329,26 @@ class Context:
             return []
         keep, rows = [], []
         any_dev = False
+        global _torch
+        if _torch is None:
+            try:
+                import torch
+                _torch = torch
+            except ImportError:
+                pass
+        T = _torch.Tensor if _torch is not None else None
+        u8 = _torch.uint8 if _torch is not None else None
         for i, (a, b) in enumerate(pairs):
-            fa = _fast_cuda(a)
-            fb = _fast_cuda(b) if fa is not None else None
-            if fb is not None:
-                if fa[1:] != fb[1:]:
-                    raise ValueError(f"pair {i}: shapes differ")
-                rows.append((fa[0], fb[0], fa[1], fa[2], fa[3], 1))
-                any_dev = True
-                continue
+            # contiguous 3-D uint8 CUDA tensors: a handful of attribute reads
+            # inline (batches touch hundreds of tensors); anything else
+            # through _Buf
+            if (type(a) is T and type(b) is T and a.dtype is u8 and b.dtype is u8 and a.is_cuda and b.is_cuda
+                    and a.is_contiguous() and b.is_contiguous()):
+                sh = a.shape
+                if len(sh) == 3 and sh == b.shape:
+                    rows.append((a.data_ptr(), b.data_ptr(), sh[2], sh[1], sh[0], 1))
+                    any_dev = True
+                    continue
             A, B = _Buf(a), _Buf(b)
             if (A.W, A.H, A.D) != (B.W, B.H, B.D) or A.on_device != B.on_device:
                 raise ValueError(f"pair {i}: shapes or devices differ")
@@ -338,7 +356,7 @@ class Context:
             any_dev = any_dev or A.on_device
             rows.append((A.ptr, B.ptr, A.W, A.H, A.D, 1 if A.on_device else 0))
         descs = np.zeros(n, dtype=_PAIR_DESC_DTYPE)
-        cols = list(zip(*rows))
+        cols = np.array(rows, dtype=np.int64).T
         descs["a"], descs["b"] = cols[0], cols[1]
         descs["W"], descs["H"], descs["D"] = cols[2], cols[3], cols[4]
         descs["metric"] = metric_code(metric)
@@ -471,6 +489,19 @@ class Server:
             raise HDError(code, "hd_server_wait")
         self._keep.pop(ticket, None)
         return r.as_dict()
+
+    def wait_any(self, timeout_ms: int = -1):
+        """(ticket, result) of the earliest finished request not yet taken,
+        waiting up to timeout_ms (< 0: no limit); None on timeout."""
+        r = N.HdResult()
+        t = ctypes.c_uint64(0)
+        code = N.load().hd_server_wait_any(self._h, int(timeout_ms), ctypes.byref(t), ctypes.byref(r))
+        if code == HD_ERR_NOT_READY:
+            return None
+        if code != HD_OK:
+            raise HDError(code, "hd_server_wait_any")
+        self._keep.pop(int(t.value), None)
+        return int(t.value), r.as_dict()
 
     def cancel(self, ticket: int):
         code = N.load().hd_server_cancel(self._h, ticket)

@@ -33,7 +33,8 @@ EXPORTS = (
     "hd_compute_u8_device_async", "hd_compute_u8_async", "hd_compute_u8_device_pipelined", "hd_pipeline_flush",
     "hd_batch_compute",
     "hd_profile_u8_device", "hd_distance_map_device", "hd_autotune", "hd_server_options_init",
-    "hd_server_create", "hd_server_submit", "hd_server_poll", "hd_server_wait", "hd_server_cancel",
+    "hd_server_create", "hd_server_submit", "hd_server_poll", "hd_server_wait", "hd_server_wait_any",
+    "hd_server_cancel",
     "hd_server_get_stats", "hd_server_destroy", "hd_compute_u8_device_noalloc", "hd_load_hdf5_bool", "hd_free",
 )
 
@@ -181,6 +182,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             "hd_server_submit": (st, [vp, ctypes.POINTER(HdPairDesc), u64p]),
             "hd_server_poll": (st, [vp, u64, res_p]),
             "hd_server_wait": (st, [vp, u64, ctypes.c_int64, res_p]),
+            "hd_server_wait_any": (st, [vp, ctypes.c_int64, u64p, res_p]),
             "hd_server_cancel": (st, [vp, u64]),
             "hd_server_get_stats": (st, [vp, ctypes.POINTER(HdServerStats)]),
             "hd_server_destroy": (st, [vp]),

@@ -360,6 +360,26 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         }
     }
     sh.finish();
+    if (sh.order == 1 && n > 1 && !ro.ordered && !ro.async_out) {
+        // largest pairs first (stable): their bricks take the lowest ids,
+        // their packing and set-up tiles come first and so do their entries
+        // in the first queue; results go back to the caller's order
+        std::vector<int> perm(n);
+        for (int i = 0; i < n; ++i) perm[i] = i;
+        std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) {
+            return (long long)pairs[x].W * pairs[x].H * pairs[x].D > (long long)pairs[y].W * pairs[y].H * pairs[y].D;
+        });
+        std::vector<PairIn> pp(n);
+        for (int i = 0; i < n; ++i) pp[i] = pairs[perm[i]];
+        std::vector<hd_result> tmp(n);
+        RunOpts r2 = ro;
+        r2.force_shape = true;
+        r2.shape = sh;
+        r2.ordered = true;
+        const hd_status st = run_pairs(ctx, pp.data(), n, s, r2, tmp.data());
+        for (int i = 0; i < n; ++i) out[perm[i]] = tmp[i];
+        return st;
+    }
     const void* solve_fn = solve_fn_of(se, sh);
     if (!solve_fn)
         return set_error(ctx, HD_ERR_BAD_ARG, "kernel %d with %d words x %d rows x %d planes (%d steps) not compiled in",
@@ -379,8 +399,10 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     const size_t off_infos = take(sizeof(PairInfo) * n);
     const size_t off_descs = take(sizeof(PairDesc) * n);
     const size_t upload_bytes = cur;           // [ctl .. descs]
-    const size_t readback_bytes = off_descs;   // [ctl .. infos]
     const size_t off_jobs = take(sizeof(Job) * 2 * n);
+    // results decoded by the persistent launch (synchronous calls read them
+    // back; asynchronous ones write to the caller's array instead)
+    const size_t off_out = take(sizeof(hd_result) * n);
     size_t hist_words = 0;
     unsigned long long total_bricks = 0;
     int kmax_all = 0;
@@ -426,7 +448,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         }
     }
     const size_t total_bytes = cur;
-    const size_t pinned_bytes = upload_bytes + sizeof(uint64_t) * (hist_words + (stats ? hist_words : 0));
+    const size_t pinned_bytes = upload_bytes + sizeof(hd_result) * n + (stats ? sizeof(uint64_t) * hist_words : 0);
 
     // Pipelined single pairs of up to 2^26 voxels run on split SMs: their
     // dilation is latency-bound and fits fewer SMs, so the next pair's
@@ -442,12 +464,22 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         if (e0 != cudaSuccess) return cuda_fail(ctx, e0, "pipeline flush");
         ctx->split.pending = false;
     }
+    // the workspace alternates only once a dilation has been launched in it
     const int ws = split ? ctx->split.next : 0;
-    if (split) ctx->split.next ^= 1;
     DeviceArena& arena = ws ? ctx->arena2 : ctx->arena;
     cudaStream_t sq = split ? ctx->split.prep : s, sv = split ? ctx->split.solve : s;
     const int prep_sms = split ? ctx->split.prep_sms : ctx->sm_count;
+    // Growing a buffer frees the old one after cudaDeviceSynchronize, which
+    // waits for the primary context's streams only: the split path's streams
+    // belong to green contexts and may still use it, so drain them first.
+    auto drain_split = [&]() {
+        if (ctx->split.state > 0) {
+            cudaStreamSynchronize(ctx->split.solve);
+            cudaStreamSynchronize(ctx->split.prep);
+        }
+    };
 
+    if (total_bytes > arena.cap) drain_split();
     cudaError_t e = arena.ensure(total_bytes);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "device workspace");
     if (split) {
@@ -460,12 +492,14 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     }
     if (total_bricks > ctx->stamp_slots || ctx->g_next > (1 << 30)) {
         const size_t want = std::max<size_t>(total_bricks, ctx->stamp_slots);
+        if (sizeof(int32_t) * want > ctx->stamps.cap) drain_split();
         e = ctx->stamps.ensure(sizeof(int32_t) * want);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "brick stamps");
         // the stamps belong to every dilation of the context: the reset
-        // follows the last one (split path: the other workspace's) and
-        // precedes this call's
-        if (split) e = cudaStreamWaitEvent(sq, ctx->split.ws_free[ws ^ 1], 0);
+        // follows the latest one (split path: a dilation the caller's stream
+        // has not waited for yet; the others precede the caller event that
+        // sq waits for) and precedes this call's
+        if (split && ctx->split.pending) e = cudaStreamWaitEvent(sq, ctx->split.ws_free[ctx->split.last], 0);
         if (e == cudaSuccess) e = cudaMemsetAsync(ctx->stamps.ptr, 0, sizeof(int32_t) * want, sq);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "stamp reset");
         ctx->stamp_slots = want;
@@ -616,8 +650,12 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     e = hdk::launch_setup(ddesc, n, setup_tiles, grid_setup, djobs, dstates, dq[g0 % 3], dctl, g0, bxw, by, bz,
                           setup_mode, sq);
     if (e == cudaSuccess && split) {
+        // the dilation follows the set-up; the caller's stream follows the
+        // packing's reads of its masks (work it queues later may overwrite
+        // or free them) but not the dilation
         e = cudaEventRecord(ctx->split.prep_done, sq);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(sv, ctx->split.prep_done, 0);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ctx->split.prep_done, 0);
     }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "setup launch");
     if (ro.map_a || ro.map_b) {
@@ -641,18 +679,19 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     sp.g0 = g0;
     sp.max_iters = kmax_all / sh.steps + 2;
     sp.stats = stats ? 1 : 0;
+    sp.spread = sh.spread;
     sp.timeout_ns = ctx->opt.barrier_timeout_ns > 0 ? ctx->opt.barrier_timeout_ns : 10000000000LL;
     const int occ = occupancy_of(ctx, solve_fn, sh.threads, sh.smem);
     if (occ <= 0) return set_error(ctx, HD_ERR_CUDA, "dilation kernel cannot be made resident");
     const int per_sm = cps > 0 ? std::min(cps, occ) : occ;
     dim3 grid((split ? ctx->split.solve_sms : ctx->sm_count) * per_sm), block(sh.threads);
     const float pct = (ctx->opt.percentile > 0.f && ctx->opt.percentile <= 1.f) ? ctx->opt.percentile : 0.95f;
-    if (async) {  // the launch decodes the results on the device
-        sp.descs = ddesc;
-        sp.npairs = n;
-        sp.pct = pct;
-        sp.out = ro.async_out;
-    }
+    // the launch decodes the results on the device (one warp per pair, after
+    // its last barrier): the per-step histograms never leave the device
+    sp.descs = ddesc;
+    sp.npairs = n;
+    sp.pct = pct;
+    sp.out = async ? ro.async_out : (hd_result*)(dbase + off_out);
     void* args[] = {&sp};
     if (timing) cudaEventRecord(ctx->ev[2], s);
     e = cudaLaunchCooperativeKernel(solve_fn, grid, block, args, (size_t)sh.smem, sv);
@@ -660,6 +699,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         e = cudaEventRecord(ctx->split.ws_free[ws], sv);
         ctx->split.pending = true;
         ctx->split.last = ws;
+        ctx->split.next = ws ^ 1;
     }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "dilation launch");
     if (timing) cudaEventRecord(ctx->ev[3], s);
@@ -670,13 +710,13 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         return HD_OK;
     }
 
-    // ---- read-back ------------------------------------------------------------
-    e = cudaMemcpyAsync(hbase, dbase, readback_bytes, cudaMemcpyDeviceToHost, s);
+    // ---- read-back: the loop control and the decoded results ------------------
+    hd_result* hres = (hd_result*)(hbase + upload_bytes);
+    e = cudaMemcpyAsync(hbase + off_ctl, dbase + off_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(hbase + upload_bytes, dbase + off_hist, sizeof(uint64_t) * hist_words,
-                            cudaMemcpyDeviceToHost, s);
+        e = cudaMemcpyAsync(hres, dbase + off_out, sizeof(hd_result) * n, cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "result read-back");
-    uint64_t* htc = (uint64_t*)(hbase + upload_bytes) + hist_words;
+    uint64_t* htc = (uint64_t*)(hres + n);
     if (stats) {
         size_t o = 0;
         for (int i = 0; i < n && e == cudaSuccess; ++i)
@@ -691,9 +731,6 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     if (e != cudaSuccess) return cuda_fail(ctx, e, "dilation");
 
     const Ctl* hctl = (const Ctl*)(hbase + off_ctl);
-    const JobState* hst = (const JobState*)(hbase + off_states);
-    const PairInfo* hin = (const PairInfo*)(hbase + off_infos);
-    const uint64_t* hh = (const uint64_t*)(hbase + upload_bytes);
     ctx->g_next = std::max(ctx->g_next, hctl->g_end) + 2;
     if (timing) {
         hd_timings& T = ctx->last_timings;
@@ -709,27 +746,24 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         T.steps_per_barrier = sh.steps;
         T.brick_rows = by;
     }
-    hd_status first = HD_OK;
-    size_t hoff = 0, toff = 0;
-    for (int i = 0; i < n; ++i) {
-        const int kp1 = plan[i].kmax + 1;
-        const uint64_t* hist_ba = hh + hoff;
-        const uint64_t* hist_ab = hh + hoff + kp1;
-        hoff += 2ULL * kp1;
-        if (stats) {
-            const uint64_t* tc0 = htc + toff;
-            const uint64_t* tc1 = htc + toff + kp1;
-            toff += 2ULL * kp1;
-            if (n == 1) {
-                for (int k = 0; k < ro.tiles_len; ++k) {
-                    if (ro.tiles_ba) ro.tiles_ba[k] = k < kp1 ? tc0[k] : 0;
-                    if (ro.tiles_ab) ro.tiles_ab[k] = k < kp1 ? tc1[k] : 0;
-                }
-                if (ro.bricks) *ro.bricks = hst[2 * i].bricks + hst[2 * i + 1].bricks;
-            }
+    if (stats && n == 1) {
+        const int kp1 = plan[0].kmax + 1;
+        for (int k = 0; k < ro.tiles_len; ++k) {
+            if (ro.tiles_ba) ro.tiles_ba[k] = k < kp1 ? htc[k] : 0;
+            if (ro.tiles_ab) ro.tiles_ab[k] = k < kp1 ? htc[kp1 + k] : 0;
         }
-        const hd_status st = decode_result(hin[i], hst[2 * i], hst[2 * i + 1], hist_ab, hist_ba, kp1,
-                                           hctl->iters_run, hctl->err, pct, &out[i]);
+        if (ro.bricks) {
+            // instrumented runs only: the brick counters of the two jobs
+            JobState js[2];
+            e = cudaMemcpy(js, dbase + off_states, sizeof js, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "instrumentation read-back");
+            *ro.bricks = js[0].bricks + js[1].bricks;
+        }
+    }
+    hd_status first = HD_OK;
+    for (int i = 0; i < n; ++i) {
+        out[i] = hres[i];
+        const hd_status st = (hd_status)hres[i].status;
         if (st == HD_EMPTY_MASK && first == HD_OK) first = st;
         if (st != HD_OK && st != HD_EMPTY_MASK) {
             if (first == HD_OK || first == HD_EMPTY_MASK) first = st;

@@ -194,6 +194,7 @@ struct SolveParams {
     int32_t g0;                    // first global iteration of this launch
     int32_t max_iters;             // iterations this launch may run
     int32_t stats;                 // instrumented run
+    int32_t spread;                // queue item i goes to warp (i mod warps) numbered CTA-major (0) or SM-spread (1)
     long long timeout_ns;          // one barrier wait
     // device-side result decode at the end of the launch (asynchronous
     // entries; out == nullptr: the host decodes)
@@ -201,6 +202,14 @@ struct SolveParams {
     int32_t npairs;
     float pct;                     // robust HD percentile
     hd_result* out;                // out[i] = result of pair i
+    // serving: decode only pairs whose descriptor is live (info != null) and
+    // whose jobs have both finished; the others' out[i] is left as it is
+    int32_t decode_done_only;
+    // serving: a word the host advances while a launch runs (requests
+    // waiting for admission); once it differs from yield_gen the loop ends
+    // at the next grid barrier (null: never)
+    const int32_t* yield;
+    int32_t yield_gen;
 };
 
 }  // namespace hdk

@@ -38,6 +38,12 @@ struct Shape {  // default: the autotuner's choice on the 512x512x256, 512^3 and
     int bz = 8;
     int steps = 2;
     int ctas_per_sm = 0;
+    // queue schedule: pair order of a batch (0 = as given, 1 = largest
+    // first: its bricks get the lowest ids and lead the first queue) and the
+    // mapping of queue items to warps (0 = CTA-major: consecutive items on
+    // the warps of one CTA, 1 = spread: consecutive items on different SMs)
+    int order = 0;
+    int spread = 0;
     int threads = 128;  // CTA size of the persistent launch
     int smem = 0;       // dynamic shared memory per CTA
     void finish() {
@@ -155,6 +161,7 @@ struct RunOpts {
     Shape shape;
     hd_result* async_out = nullptr;  // device memory: enqueue only, results decoded on the device
     bool pipelined = false;          // with async_out: the result may complete after a later flush
+    bool ordered = false;            // the pairs are already in the shape's order (internal)
 };
 
 hd_status set_error(hd_context* ctx, hd_status st, const char* fmt, ...);

@@ -20,8 +20,12 @@ cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, i
 cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int grid, Job* jobs,
                          JobState* states, unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
                          int mode, cudaStream_t s);
-// Start values of descs[i].info (counts 0, empty bounding box), i < npairs.
-cudaError_t launch_info_init(const PairDesc* d_descs, int npairs, cudaStream_t s);
+// Start values of descs[i].info (counts 0, empty bounding box), i < npairs;
+// with slot_descs, also copies descs[i] to slot_descs[descs[i].job0 / 2].
+cudaError_t launch_info_init(const PairDesc* d_descs, int npairs, cudaStream_t s, PairDesc* slot_descs = nullptr);
+// Serving: list = n (slot, epoch) pairs (device memory); each slot's jobs
+// take the epoch and slot_descs[slot].info becomes null.
+cudaError_t launch_retire(Job* jobs, PairDesc* slot_descs, const uint32_t* list, int n, cudaStream_t s);
 cudaError_t launch_zero_i32(int32_t* p, long long n, cudaStream_t s);
 cudaError_t launch_map_init(const PairDesc* d_descs, int32_t* map_a, int32_t* map_b, long long n, int label,
                             cudaStream_t s);

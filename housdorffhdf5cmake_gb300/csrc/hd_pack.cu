@@ -560,14 +560,28 @@ __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_
 }
 
 // Start values of each pair's counts and bounding box (one thread per pair).
-__global__ void info_init_kernel(const PairDesc* __restrict__ descs, int npairs) {
+__global__ void info_init_kernel(const PairDesc* __restrict__ descs, int npairs, PairDesc* __restrict__ slot_descs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npairs) return;
+    if (slot_descs) slot_descs[descs[i].job0 / 2] = descs[i];  // serving: the slot's copy for the result decode
     PairInfo* I = descs[i].info;
     I->n_a = I->n_b = I->n_ab = 0ull;
     I->bb[0] = I->bb[2] = I->bb[4] = INT_MAX;
     I->bb[1] = I->bb[3] = I->bb[5] = -1;
     I->pad[0] = I->pad[1] = 0;
+}
+
+// Serving: retire finished pairs' slots.  list holds (slot, epoch) pairs: the
+// slot's jobs take the new epoch (queue entries still listed for them are
+// dropped) and the slot's descriptor copy is marked unused (info = null).
+__global__ void retire_kernel(Job* __restrict__ jobs, PairDesc* __restrict__ slot_descs,
+                              const uint32_t* __restrict__ list, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t slot = list[2 * i], ep = list[2 * i + 1];
+    jobs[2 * slot].epoch = ep;
+    jobs[2 * slot + 1].epoch = ep;
+    slot_descs[slot].info = nullptr;
 }
 
 // Instrumented runs: zero the per-tile stamps and per-step tile counters.
@@ -631,9 +645,15 @@ cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_info_init(const PairDesc* d_descs, int npairs, cudaStream_t s) {
+cudaError_t launch_info_init(const PairDesc* d_descs, int npairs, cudaStream_t s, PairDesc* slot_descs) {
     if (npairs <= 0) return cudaSuccess;
-    info_init_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(d_descs, npairs);
+    info_init_kernel<<<(npairs + 255) / 256, 256, 0, s>>>(d_descs, npairs, slot_descs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_retire(Job* jobs, PairDesc* slot_descs, const uint32_t* list, int n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    retire_kernel<<<(n + 127) / 128, 128, 0, s>>>(jobs, slot_descs, list, n);
     return cudaGetLastError();
 }
 

@@ -130,8 +130,18 @@ struct hd_server {
     PairDesc* d_descs = nullptr;      // per-tick admission descriptors
     int max_admit = 256;
     cudaMemPool_t pool = nullptr;     // the pairs' buffers: a private pool that keeps what it has reserved
-    void* h_pinned = nullptr;         // descriptors out, states in
+    void* h_pinned = nullptr;         // descriptors and retirements out, states and results in
     size_t h_pinned_bytes = 0;
+    size_t off_h_results = 0, off_h_retire = 0, off_h_yield = 0;
+    PairDesc* d_slot_descs = nullptr; // per slot: its pair's descriptor (info = null: unused)
+    hd_result* d_results = nullptr;   // per slot: the result decoded by the launch that finished it
+    uint32_t* d_retire = nullptr;     // (slot, epoch) pairs retired by a tick
+    int32_t* d_yield = nullptr;       // yield generation, advanced by submissions during a tick
+    cudaStream_t side = nullptr;      // posts the yield word while a tick runs
+    cudaEvent_t ev_yield = nullptr;
+    int32_t yield_gen = 0;            // last generation posted
+    bool in_tick = false, yield_posted = false;
+    std::deque<uint64_t> done_order;  // tickets in completion order (hd_server_wait_any)
     int g_next = 1;
     hd_server_stats stats{};
     std::string err;
@@ -168,11 +178,19 @@ void plan_request(hd_server* s, Request* r) {
     r->transient_bytes = 2 * packed + (r->dev_a ? 0 : 2 * align_up(nb));
 }
 
-void complete(hd_server* s, Request* r, hd_status st) {
+// Marks a request done (server lock held) and lists it for wait_any.
+void mark_done(hd_server* s, Request* r) {
     r->state = kDone;
+    // tickets taken by poll / wait leave the completion list from its front
+    while (!s->done_order.empty() && !s->reqs.count(s->done_order.front())) s->done_order.pop_front();
+    s->done_order.push_back(r->ticket);
+}
+
+void complete(hd_server* s, Request* r, hd_status st) {
     r->result.status = st;
-    if (st != HD_OK && st != HD_EMPTY_MASK) r->result.hd = -1;
+    if (st != HD_OK && st != HD_EMPTY_MASK) r->result.hd = r->result.hd_ab = r->result.hd_ba = r->result.hd_robust = -1;
     s->stats.completed += 1;
+    mark_done(s, r);
 }
 
 // One scheduler tick.  Called with the server lock NOT held.
@@ -180,13 +198,15 @@ void tick(hd_server* s) {
     using clk = std::chrono::steady_clock;
     const auto t_begin = clk::now();
     std::vector<Request*> admit;
+    int32_t ygen = 0;
+    int used_hi = 0;  // slots [0, used_hi) hold every resident pair
     {
         std::lock_guard<std::mutex> lk(s->mu);
         // cancelled waiting requests leave at once
         for (auto it = s->waiting.begin(); it != s->waiting.end();) {
             if ((*it)->cancel) {
                 (*it)->result.status = HD_ERR_CANCELLED;
-                (*it)->state = kDone;
+                mark_done(s, *it);
                 s->stats.cancelled += 1;
                 it = s->waiting.erase(it);
             } else {
@@ -200,9 +220,7 @@ void tick(hd_server* s) {
             const size_t need = r->resident_bytes + r->transient_bytes;
             if (need > s->opt.hbm_budget_bytes) {  // can never fit
                 s->waiting.pop_front();
-                r->result.status = HD_ERR_OOM;
-                r->state = kDone;
-                s->stats.completed += 1;
+                complete(s, r, HD_ERR_OOM);
                 continue;
             }
             if (s->stats.bytes_in_use + need > s->opt.hbm_budget_bytes) break;
@@ -218,6 +236,14 @@ void tick(hd_server* s) {
             s->stats.bytes_peak = std::max(s->stats.bytes_peak, s->stats.bytes_in_use);
             admit.push_back(r);
         }
+        // submissions from here on advance the yield word (once per tick):
+        // this tick's launch then ends at its next barrier so that they are
+        // admitted by the next tick
+        s->in_tick = true;
+        s->yield_posted = false;
+        ygen = s->yield_gen;
+        for (size_t sl = 0; sl < s->slots.size(); ++sl)
+            if (s->slots[sl]) used_hi = (int)sl + 1;
         s->done_cv.notify_all();
     }
     cudaStream_t st = s->stream;
@@ -294,7 +320,7 @@ void tick(hd_server* s) {
         char* hp = (char*)s->h_pinned + align_up(sizeof(Ctl)) + align_up(sizeof(JobState) * 2 * s->slots.size());
         std::memcpy(hp, descs.data(), sizeof(PairDesc) * descs.size());
         e = cudaMemcpyAsync(s->d_descs, hp, sizeof(PairDesc) * descs.size(), cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = hdk::launch_info_init(s->d_descs, (int)descs.size(), st);
+        if (e == cudaSuccess) e = hdk::launch_info_init(s->d_descs, (int)descs.size(), st, s->d_slot_descs);
         const int cap_ctas = std::max(s->ctx->sm_count * 8, 1);
         if (e == cudaSuccess)
             e = hdk::launch_pack(s->d_descs, (int)admitted.size(), ptiles, (int)std::min<long long>(cap_ctas, ptiles),
@@ -322,6 +348,7 @@ void tick(hd_server* s) {
     // ---- one tick of the persistent dilation loop ---------------------------
     int resident = 0;
     for (auto* r : s->slots) resident += r != nullptr;
+    const float pct = (s->ctx->opt.percentile > 0.f && s->ctx->opt.percentile <= 1.f) ? s->ctx->opt.percentile : 0.95f;
     if (resident > 0 && e == cudaSuccess) {
         hdk::SolveParams sp{};
         sp.jobs = s->d_jobs;
@@ -332,19 +359,38 @@ void tick(hd_server* s) {
         sp.g0 = s->g_next;
         sp.max_iters = s->opt.tick_iterations;
         sp.timeout_ns = s->ctx->opt.barrier_timeout_ns > 0 ? s->ctx->opt.barrier_timeout_ns : 10000000000LL;
+        // after its last barrier the launch decodes every pair that has
+        // finished into its slot's result (the histograms stay on the device)
+        sp.descs = s->d_slot_descs;
+        sp.npairs = used_hi;
+        sp.pct = pct;
+        sp.out = s->d_results;
+        sp.decode_done_only = 1;
+        sp.yield = s->d_yield;
+        sp.yield_gen = ygen;
         void* args[] = {&sp};
-        e = cudaLaunchCooperativeKernel(s->solve_fn, dim3(s->grid), dim3(s->shape.threads), args,
-                                        (size_t)s->shape.smem, st);
+        // yield words posted before this tick have landed
+        e = cudaStreamWaitEvent(st, s->ev_yield, 0);
+        if (e == cudaSuccess)
+            e = cudaLaunchCooperativeKernel(s->solve_fn, dim3(s->grid), dim3(s->shape.threads), args,
+                                            (size_t)s->shape.smem, st);
     }
-    // ---- read back states, complete finished pairs ---------------------------
-    const size_t nst = 2 * s->slots.size();
+    // ---- read back loop control, job states and results, in one wait ---------
+    const size_t nst = 2 * (size_t)used_hi;
     char* hp = (char*)s->h_pinned;
     Ctl* hctl = (Ctl*)hp;
     JobState* hst = (JobState*)(hp + align_up(sizeof(Ctl)));
+    hd_result* hres = (hd_result*)(hp + s->off_h_results);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hctl, s->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && nst)
         e = cudaMemcpyAsync(hst, s->d_states, sizeof(JobState) * nst, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && used_hi)
+        e = cudaMemcpyAsync(hres, s->d_results, sizeof(hd_result) * used_hi, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->in_tick = false;
+    }
     int hard_err = 0;
     if (e != cudaSuccess) {
         cuda_err(s, e, "tick");
@@ -377,7 +423,7 @@ void tick(hd_server* s) {
                          hctl->iters_run == 0 && hctl->jobs_active > 0;
     if (stalled && s->debug) std::fprintf(stderr, "[hd_server] no progress: failing active pairs\n");
     std::vector<Request*> finished;
-    for (size_t sl = 0; sl < s->slots.size(); ++sl) {
+    for (size_t sl = 0; sl < (size_t)used_hi; ++sl) {
         Request* r = s->slots[sl];
         if (!r) continue;
         const JobState& s0 = hst[2 * sl];
@@ -387,6 +433,8 @@ void tick(hd_server* s) {
     }
     if (stalled) hard_err = HD_ERR_ITER_LIMIT;
     unsigned long long cancelled_active = 0;
+    uint32_t* hretire = (uint32_t*)(hp + s->off_h_retire);
+    int nretire = 0;
     for (Request* r : finished) {
         const size_t sl = (size_t)r->slot;
         const JobState s0 = hst[2 * sl], s1 = hst[2 * sl + 1];
@@ -395,29 +443,23 @@ void tick(hd_server* s) {
             st_r = HD_ERR_CANCELLED;
             cancelled_active += (s0.active != 0) + (s1.active != 0);
             r->result = hd_result{};
+        } else if (hard_err) {
+            r->result = hd_result{};
+            st_r = (hd_status)hard_err;
         } else {
-            const int kp1 = r->kmax + 1;
-            std::vector<uint64_t> hist(2 * kp1);
-            PairInfo info{};
-            cudaError_t e2 = cudaMemcpyAsync(hist.data(), (char*)r->resident + r->off_hist,
-                                             sizeof(uint64_t) * 2 * kp1, cudaMemcpyDeviceToHost, st);
-            if (e2 == cudaSuccess)
-                e2 = cudaMemcpyAsync(&info, (char*)r->resident + r->off_info, sizeof info, cudaMemcpyDeviceToHost, st);
-            if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(st);
-            const float pct = (s->ctx->opt.percentile > 0.f && s->ctx->opt.percentile <= 1.f) ? s->ctx->opt.percentile : 0.95f;
-            if (e2 != cudaSuccess) {
-                cudaGetLastError();
-                st_r = HD_ERR_CUDA;
-            } else {
-                st_r = decode_result(info, s0, s1, hist.data() + kp1, hist.data(), kp1, 0, hard_err, pct, &r->result);
-            }
+            // decoded on the device at the end of this tick's launch (the
+            // rules of decode_result: statuses, exact sums, one division,
+            // robust HD from the per-step histogram)
+            r->result = hres[sl];
+            st_r = (hd_status)r->result.status;
         }
         // Queue entries of the finished jobs may still be waiting for the
         // next step: a new epoch on the jobs makes the kernels drop them
-        // before they read the buffers freed here (the byte fills the whole
-        // epoch word; entries compare its low 8 bits).
-        const unsigned dead = ++s->slot_epoch[sl] & 0xffu;
-        for (int j = 0; j < 2; ++j) cudaMemsetAsync(&s->d_jobs[2 * sl + j].epoch, (int)dead, sizeof(uint32_t), st);
+        // before they read the buffers freed here (entries compare the low
+        // 8 bits), and the slot's descriptor copy is marked unused.
+        hretire[2 * nretire] = (uint32_t)sl;
+        hretire[2 * nretire + 1] = ++s->slot_epoch[sl];
+        ++nretire;
         cudaFreeAsync(r->resident, st);
         r->resident = nullptr;
         std::lock_guard<std::mutex> lk(s->mu);
@@ -427,11 +469,19 @@ void tick(hd_server* s) {
         s->quarantine.push_back((int)sl);
         if (r->cancel) {
             r->result.status = HD_ERR_CANCELLED;
-            r->state = kDone;
+            mark_done(s, r);
             s->stats.cancelled += 1;
         } else {
             complete(s, r, st_r);
         }
+    }
+    if (nretire) {
+        // the list is read before the next tick rewrites it (the end of
+        // every tick waits for the stream)
+        cudaError_t e3 = cudaMemcpyAsync(s->d_retire, hretire, sizeof(uint32_t) * 2 * nretire,
+                                         cudaMemcpyHostToDevice, st);
+        if (e3 == cudaSuccess) e3 = hdk::launch_retire(s->d_jobs, s->d_slot_descs, s->d_retire, nretire, st);
+        if (e3 != cudaSuccess) cuda_err(s, e3, "retire");
     }
     if (cancelled_active || hard_err) {
         // Cancelled jobs leave the loop: mark them inactive and fix the
@@ -489,7 +539,7 @@ void hd_server_options_init(hd_server_options* opt) {
     std::memset(opt, 0, sizeof *opt);
     opt->hbm_budget_bytes = 120ULL << 30;
     opt->max_queue = 4096;
-    opt->tick_iterations = 16;
+    opt->tick_iterations = 64;
     opt->metric = HD_SE6;
 }
 
@@ -503,7 +553,7 @@ hd_status hd_server_create(hd_context* ctx, const hd_server_options* opt, hd_ser
     if (opt) s->opt = *opt;
     if (!s->opt.hbm_budget_bytes) s->opt.hbm_budget_bytes = 120ULL << 30;
     if (s->opt.max_queue <= 0) s->opt.max_queue = 4096;
-    if (s->opt.tick_iterations <= 0) s->opt.tick_iterations = 16;
+    if (s->opt.tick_iterations <= 0) s->opt.tick_iterations = 64;
     if (s->opt.metric != HD_SE6 && s->opt.metric != HD_SE18_FORBENCH) {
         delete s;
         return HD_ERR_BAD_ARG;
@@ -558,11 +608,23 @@ hd_status hd_server_create(hd_context* ctx, const hd_server_options* opt, hd_ser
             e = cudaMalloc(&s->d_queue[q], sizeof(unsigned long long) * s->brick_cap);
         if (e == cudaSuccess) e = cudaMalloc(&s->d_stamps, sizeof(int32_t) * s->brick_cap);
         if (e == cudaSuccess) e = cudaMalloc(&s->d_descs, sizeof(PairDesc) * s->max_admit);
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_slot_descs, sizeof(PairDesc) * slots);
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_results, sizeof(hd_result) * slots);
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_retire, sizeof(uint32_t) * 2 * slots);
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_yield, sizeof(int32_t));
         if (e == cudaSuccess) e = cudaMemset(s->d_states, 0, sizeof(JobState) * 2 * slots);
         if (e == cudaSuccess) e = cudaMemset(s->d_ctl, 0, sizeof(Ctl));
         if (e == cudaSuccess) e = cudaMemset(s->d_stamps, 0, sizeof(int32_t) * s->brick_cap);
-        s->h_pinned_bytes = align_up(sizeof(Ctl)) + align_up(sizeof(JobState) * 2 * slots) +
-                            sizeof(PairDesc) * s->max_admit;
+        if (e == cudaSuccess) e = cudaMemset(s->d_slot_descs, 0, sizeof(PairDesc) * slots);  // info = null: unused
+        if (e == cudaSuccess) e = cudaMemset(s->d_yield, 0, sizeof(int32_t));
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_yield, cudaEventDisableTiming);
+        // pinned: [Ctl][JobState x 2 slots][PairDesc x max_admit][hd_result x slots][retire list][yield word]
+        s->off_h_results = align_up(align_up(sizeof(Ctl)) + align_up(sizeof(JobState) * 2 * slots) +
+                                    sizeof(PairDesc) * s->max_admit);
+        s->off_h_retire = align_up(s->off_h_results + sizeof(hd_result) * slots);
+        s->off_h_yield = align_up(s->off_h_retire + sizeof(uint32_t) * 2 * slots);
+        s->h_pinned_bytes = s->off_h_yield + sizeof(int32_t);
         if (e == cudaSuccess) e = cudaHostAlloc(&s->h_pinned, s->h_pinned_bytes, cudaHostAllocDefault);
         if (e != cudaSuccess) {
             cudaGetLastError();
@@ -602,6 +664,19 @@ hd_status hd_server_submit(hd_server* s, const hd_pair_desc* pair, uint64_t* tic
     s->waiting.push_back(r.get());
     s->reqs[r->ticket] = std::move(r);
     s->stats.submitted += 1;
+    if (s->in_tick && !s->yield_posted) {
+        // a tick is running: advance the yield word so that its launch ends
+        // at the next grid barrier and the next tick admits this request.
+        // The copy may read a later (larger) generation than the one written
+        // here, which ends the launch just the same.
+        s->yield_posted = true;
+        int32_t* hy = (int32_t*)((char*)s->h_pinned + s->off_h_yield);
+        *hy = ++s->yield_gen;
+        DeviceGuard g(s->ctx->device);
+        cudaError_t e = cudaMemcpyAsync(s->d_yield, hy, sizeof(int32_t), cudaMemcpyHostToDevice, s->side);
+        if (e == cudaSuccess) e = cudaEventRecord(s->ev_yield, s->side);
+        if (e != cudaSuccess) cudaGetLastError();  // the tick then simply runs to its end
+    }
     s->cv.notify_all();
     return HD_OK;
 }
@@ -631,6 +706,28 @@ hd_status hd_server_wait(hd_server* s, uint64_t ticket, int64_t timeout_ms, hd_r
     }
     *out = r->result;
     s->reqs.erase(ticket);
+    return HD_OK;
+}
+
+hd_status hd_server_wait_any(hd_server* s, int64_t timeout_ms, uint64_t* ticket, hd_result* out) {
+    if (!s || !ticket || !out) return HD_ERR_BAD_ARG;
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+        // tickets already taken by hd_server_poll / hd_server_wait are skipped
+        while (!s->done_order.empty() && !s->reqs.count(s->done_order.front())) s->done_order.pop_front();
+        if (!s->done_order.empty()) break;
+        auto ready = [&] { return !s->done_order.empty(); };
+        if (timeout_ms < 0) {
+            s->done_cv.wait(lk, ready);
+        } else if (!s->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
+            return HD_ERR_NOT_READY;
+        }
+    }
+    const uint64_t t = s->done_order.front();
+    s->done_order.pop_front();
+    *ticket = t;
+    *out = s->reqs[t]->result;
+    s->reqs.erase(t);
     return HD_OK;
 }
 
@@ -676,6 +773,15 @@ hd_status hd_server_destroy(hd_server* s) {
         for (auto* q : s->d_queue) cudaFree(q);
         cudaFree(s->d_stamps);
         cudaFree(s->d_descs);
+        cudaFree(s->d_slot_descs);
+        cudaFree(s->d_results);
+        cudaFree(s->d_retire);
+        cudaFree(s->d_yield);
+        if (s->side) {
+            cudaStreamSynchronize(s->side);
+            cudaStreamDestroy(s->side);
+        }
+        if (s->ev_yield) cudaEventDestroy(s->ev_yield);
         if (s->h_pinned) cudaFreeHost(s->h_pinned);
         if (s->stream) cudaStreamDestroy(s->stream);
         cudaGetLastError();

@@ -76,12 +76,12 @@ constexpr int kErrIterLimit = 7;  // HD_ERR_ITER_LIMIT
 
 // Grid-wide barrier for a cooperative launch.  The last CTA to arrive
 // decides whether the loop continues (no error, jobs left, next queue not
-// empty), resets the queue counter that step g + 2 will fill, and releases
-// the others.  Every wait is bounded: after timeout_ns (or 2^26 polls) the
+// empty, no yield requested through `yield`), resets the queue counter that
+// step g + 2 will fill, and releases the others.  Every wait is bounded: after timeout_ns (or 2^26 polls) the
 // waiting CTA records HD_ERR_TIMEOUT and leaves, and every other waiter sees
 // the error and leaves as well.  Returns the continue flag (CTA-uniform).
 __device__ __forceinline__ bool grid_step_barrier(Ctl* ctl, unsigned& gen, int g, long long timeout_ns, int* s_flag,
-                                                  unsigned* s_cnt) {
+                                                  unsigned* s_cnt, const int32_t* yield, int32_t yield_gen) {
     __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned target = gen + 1u;
@@ -95,7 +95,8 @@ __device__ __forceinline__ bool grid_step_barrier(Ctl* ctl, unsigned& gen, int g
             const int err = ld_relaxed_s32(&ctl->err);
             const int jobs = ld_relaxed_s32(&ctl->jobs_active);
             const unsigned nq = ld_relaxed_u32(&ctl->qcount[(g + 1) % 3]);
-            const bool cont = err == 0 && jobs > 0 && nq > 0u;
+            const bool yl = yield != nullptr && ld_relaxed_s32(yield) != yield_gen;
+            const bool cont = err == 0 && jobs > 0 && nq > 0u && !yl;
             ctl->qcount[(g + 2) % 3] = 0u;
             rel = ((unsigned long long)target << 32) | (cont ? 0x80000000ull : 0ull) | (nq & 0x7fffffffu);
             atom_exch_release_u64(&ctl->release, rel);
@@ -157,6 +158,10 @@ __device__ __forceinline__ int robust_k_warp(const unsigned long long* hist, int
 // when every job's state is final.
 static __device__ __noinline__ void decode_pair_warp(const SolveParams& p, int i, int iters) {
     const PairDesc& P = p.descs[i];
+    if (p.decode_done_only) {
+        if (P.info == nullptr) return;  // slot not in use
+        if (p.states[P.job0].active != 0 || p.states[P.job0 + 1].active != 0) return;  // still running
+    }
     const PairInfo I = *P.info;
     const JobState s0 = p.states[P.job0], s1 = p.states[P.job0 + 1];
     hd_result r;
@@ -423,7 +428,9 @@ __global__ void __launch_bounds__(256, 2) solve_kernel(SolveParams p) {
     unsigned gen = s_gen;
     unsigned cnt = s_cnt;
     const int wpb = blockDim.x >> 5;
-    const unsigned gw = blockIdx.x * wpb + (threadIdx.x >> 5);
+    // warp number: CTA-major (consecutive queue items on one CTA's warps,
+    // neighbouring bricks share halo lines in L1) or spread over the SMs
+    const unsigned gw = p.spread ? (threadIdx.x >> 5) * gridDim.x + blockIdx.x : blockIdx.x * wpb + (threadIdx.x >> 5);
     const unsigned nw = gridDim.x * wpb;
     int g = p.g0;
     int it = 0;
@@ -435,7 +442,7 @@ __global__ void __launch_bounds__(256, 2) solve_kernel(SolveParams p) {
                 const unsigned long long e = Q[i];
                 brick_step<BXW, BZ, SE18>(p, (int)((e >> 32) & 0xffffffu), (unsigned)e, (unsigned)(e >> 56), g);
             }
-            const bool cont = grid_step_barrier(ctl, gen, g, p.timeout_ns, &s_flag, &s_cnt);
+            const bool cont = grid_step_barrier(ctl, gen, g, p.timeout_ns, &s_flag, &s_cnt, p.yield, p.yield_gen);
             ++g;
             ++it;
             if (!cont || it >= p.max_iters) break;

@@ -534,7 +534,9 @@ __global__ void __launch_bounds__(kTbWarps * 32, kTbMinCtas) solve_tb_kernel(Sol
     unsigned gen = s_gen;
     unsigned cnt = s_cnt;
     const int wpb = blockDim.x >> 5;
-    const unsigned gw = blockIdx.x * wpb + (threadIdx.x >> 5);
+    // warp number: CTA-major (consecutive queue items on one CTA's warps,
+    // neighbouring bricks share halo lines in L1) or spread over the SMs
+    const unsigned gw = p.spread ? (threadIdx.x >> 5) * gridDim.x + blockIdx.x : blockIdx.x * wpb + (threadIdx.x >> 5);
     const unsigned nw = gridDim.x * wpb;
     int g = p.g0;
     int it = 0;
@@ -561,7 +563,7 @@ __global__ void __launch_bounds__(kTbWarps * 32, kTbMinCtas) solve_tb_kernel(Sol
                 cur = nxt;
                 i = in;
             }
-            const bool cont = grid_step_barrier(ctl, gen, g, p.timeout_ns, &s_flag, &s_cnt);
+            const bool cont = grid_step_barrier(ctl, gen, g, p.timeout_ns, &s_flag, &s_cnt, p.yield, p.yield_gen);
             ++g;
             ++it;
             if (!cont || it >= p.max_iters) break;

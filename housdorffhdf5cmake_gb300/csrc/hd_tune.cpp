@@ -1,11 +1,13 @@
-// hd_tune.cpp -- autotuner for brick shape and persistent-grid size.
+// hd_tune.cpp -- autotuner for brick shape, persistent-grid size and queue
+// schedule.
 //
 // Replaces the reference's launch-shape choice by the occupancy API
 // (getOccupancy, hello.cu:1910-1954), whose data-block y size even follows
 // the occupancy result (hello.cu:917).  Here the data layout never depends on
-// the GPU; only the brick shape (words x rows x planes per warp) and the
-// number of resident CTAs per SM are searched, by timing real runs on the
-// caller's pairs.  Winners are kept per workload class and can be persisted
+// the GPU; the brick shape (words x rows x planes per warp), the number of
+// resident CTAs per SM and the queue schedule (pair order of a batch, mapping
+// of queue items to warps) are searched, by timing real runs on the caller's
+// pairs.  Winners are kept per workload class and can be persisted
 // as a small JSON table.
 #include <cuda_runtime.h>
 
@@ -42,7 +44,8 @@ bool TuneTable::save(const std::string& path) const {
         const Shape& sh = kv.second.shape;
         f << (first ? "\n" : ",\n") << "    \"" << kv.first << "\": {\"kernel\": " << sh.kernel
           << ", \"bxw\": " << sh.bxw << ", \"bz\": " << sh.bz << ", \"steps\": " << sh.steps
-          << ", \"ctas_per_sm\": " << sh.ctas_per_sm << ", \"us\": " << kv.second.us << "}";
+          << ", \"ctas_per_sm\": " << sh.ctas_per_sm << ", \"order\": " << sh.order
+          << ", \"spread\": " << sh.spread << ", \"us\": " << kv.second.us << "}";
         first = false;
     }
     f << "\n  }\n}\n";
@@ -77,11 +80,13 @@ bool TuneTable::load(const std::string& path) {
         if (k1 == std::string::npos || b0 == std::string::npos || b1 == std::string::npos) break;
         const std::string key = s.substr(k0 + 1, k1 - k0 - 1);
         const std::string body = s.substr(b0, b1 - b0 + 1);
-        double kernel = 1, bxw = 0, bz = 0, steps = 1, cps = 0, us = 0;
+        double kernel = 1, bxw = 0, bz = 0, steps = 1, cps = 0, order = 0, spread = 0, us = 0;
         if (field(body, "bxw", &bxw) && field(body, "bz", &bz)) {
             field(body, "kernel", &kernel);
             field(body, "steps", &steps);
             field(body, "ctas_per_sm", &cps);
+            field(body, "order", &order);
+            field(body, "spread", &spread);
             field(body, "us", &us);
             TuneEntry e;
             e.shape.kernel = (int)kernel;
@@ -89,6 +94,8 @@ bool TuneTable::load(const std::string& path) {
             e.shape.bz = (int)bz;
             e.shape.steps = (int)steps;
             e.shape.ctas_per_sm = (int)cps;
+            e.shape.order = order != 0 ? 1 : 0;
+            e.shape.spread = spread != 0 ? 1 : 0;
             e.shape.finish();
             e.us = us;
             entries[key] = e;
@@ -128,8 +135,60 @@ extern "C" hd_status hd_autotune(hd_context* ctx, const hd_pair_desc* pairs, int
     }
     repeats = std::max(1, repeats);
     std::vector<hd_result> res(n), ref(n);
-    // candidates: the one-step kernel over its brick shapes, the blocked
-    // kernel over steps per barrier and depth, each at two grid sizes
+    // every field but `iterations` (the barrier count depends on the shape)
+    // must agree across candidates; avg_hd bit for bit (NaN included)
+    auto differs = [](const hd_result& x, const hd_result& y) {
+        return x.hd != y.hd || x.hd_ab != y.hd_ab || x.hd_ba != y.hd_ba || x.hd_robust != y.hd_robust ||
+               x.sum_ab != y.sum_ab || x.sum_ba != y.sum_ba || x.n_a != y.n_a || x.n_b != y.n_b ||
+               x.n_a_not_b != y.n_a_not_b || x.n_b_not_a != y.n_b_not_a || x.status != y.status ||
+               std::memcmp(&x.avg_hd, &y.avg_hd, sizeof(double)) != 0;
+    };
+    std::string rep;
+    bool have_ref = false;
+    // Runs one candidate: a warm-up run checked against the first
+    // candidate's results, then `repeats` timed runs (host clock around the
+    // whole call, which ends with the results on the host); median.
+    auto measure = [&](const Shape& c, double* med) -> hd_status {
+        RunOpts ro;
+        ro.se = se;
+        ro.force_shape = true;
+        ro.shape = c;
+        hd_status st = run_pairs(ctx, in.data(), n, ctx->stream, ro, res.data());
+        if (st != HD_OK && st != HD_EMPTY_MASK) return st;
+        if (!have_ref) {
+            ref = res;
+            have_ref = true;
+        } else {
+            for (int i = 0; i < n; ++i)
+                if (differs(res[i], ref[i]))
+                    return set_error(ctx, HD_ERR_CUDA,
+                                     "autotune: kernel %d shape %dx%dx%d steps %d order %d spread %d gave a different "
+                                     "result on pair %d (hd %d/%d/%d sums %llu/%llu, first shape: hd %d/%d/%d sums "
+                                     "%llu/%llu)",
+                                     c.kernel, c.bxw, c.by, c.bz, c.steps, c.order, c.spread, i, res[i].hd,
+                                     res[i].hd_ab, res[i].hd_ba, (unsigned long long)res[i].sum_ab,
+                                     (unsigned long long)res[i].sum_ba, ref[i].hd, ref[i].hd_ab, ref[i].hd_ba,
+                                     (unsigned long long)ref[i].sum_ab, (unsigned long long)ref[i].sum_ba);
+        }
+        std::vector<double> t;
+        for (int r = 0; r < repeats; ++r) {
+            const auto t0 = std::chrono::steady_clock::now();
+            st = run_pairs(ctx, in.data(), n, ctx->stream, ro, res.data());
+            const auto t1 = std::chrono::steady_clock::now();
+            if (st != HD_OK && st != HD_EMPTY_MASK) return st;
+            t.push_back(std::chrono::duration<double, std::micro>(t1 - t0).count());
+        }
+        std::sort(t.begin(), t.end());
+        *med = t[t.size() / 2];
+        char line[200];
+        std::snprintf(line, sizeof line, "kernel=%d bxw=%d by=%d bz=%d steps=%d cps=%d order=%d spread=%d: %.1f us\n",
+                      c.kernel, c.bxw, c.by, c.bz, c.steps, c.ctas_per_sm, c.order, c.spread, *med);
+        rep += line;
+        return HD_OK;
+    };
+    // Stage 1, kernels and bricks: the one-step kernel over its brick
+    // shapes, the blocked kernel over steps per barrier and depth, each at
+    // two grid sizes, with the default queue schedule.
     std::vector<Shape> cands;
     for (int bxw : {2, 4, 8})
         for (int bz : {4, 8, 16}) {
@@ -148,61 +207,53 @@ extern "C" hd_status hd_autotune(hd_context* ctx, const hd_pair_desc* pairs, int
             c.bz = bz;
             cands.push_back(c);
         }
-    TuneEntry best;
-    best.us = 1e300;
-    std::string rep;
-    bool have_ref = false;
+    std::vector<std::pair<double, Shape>> scored;
     for (Shape c : cands) {
         for (int cps : {0, 1}) {
             c.ctas_per_sm = cps;
+            c.order = c.spread = 0;
             c.finish();
-            RunOpts ro;
-            ro.se = se;
-            ro.force_shape = true;
-            ro.shape = c;
-            hd_status st = run_pairs(ctx, in.data(), n, ctx->stream, ro, res.data());  // warm-up
-            if (st != HD_OK && st != HD_EMPTY_MASK) return st;
-            if (!have_ref) {
-                ref = res;
-                have_ref = true;
-            } else {
-                for (int i = 0; i < n; ++i)
-                    if (res[i].hd != ref[i].hd || res[i].sum_ab != ref[i].sum_ab || res[i].sum_ba != ref[i].sum_ba)
-                        return set_error(ctx, HD_ERR_CUDA,
-                                         "autotune: kernel %d shape %dx%dx%d steps %d gave a different result on pair %d "
-                                         "(hd %d sums %llu/%llu, first shape: hd %d sums %llu/%llu)",
-                                         c.kernel, c.bxw, c.by, c.bz, c.steps, i, res[i].hd,
-                                         (unsigned long long)res[i].sum_ab, (unsigned long long)res[i].sum_ba, ref[i].hd,
-                                         (unsigned long long)ref[i].sum_ab, (unsigned long long)ref[i].sum_ba);
-            }
-            std::vector<double> t;
-            for (int r = 0; r < repeats; ++r) {
-                const auto t0 = std::chrono::steady_clock::now();
-                st = run_pairs(ctx, in.data(), n, ctx->stream, ro, res.data());
-                const auto t1 = std::chrono::steady_clock::now();
-                if (st != HD_OK && st != HD_EMPTY_MASK) return st;
-                t.push_back(std::chrono::duration<double, std::micro>(t1 - t0).count());
-            }
-            std::sort(t.begin(), t.end());
-            const double med = t[t.size() / 2];
-            char line[160];
-            std::snprintf(line, sizeof line, "kernel=%d bxw=%d by=%d bz=%d steps=%d cps=%d: %.1f us\n", c.kernel, c.bxw,
-                          c.by, c.bz, c.steps, cps, med);
-            rep += line;
-            if (med < best.us) {
-                best.us = med;
-                best.shape = c;
-            }
+            double med = 0;
+            const hd_status st = measure(c, &med);
+            if (st != HD_OK) return st;
+            scored.emplace_back(med, c);
         }
     }
+    // Stage 2, queue schedule on the three fastest: pair order (as given /
+    // largest first) x item-to-warp mapping (CTA-major / spread over SMs).
+    std::stable_sort(scored.begin(), scored.end(),
+                     [](const std::pair<double, Shape>& x, const std::pair<double, Shape>& y) { return x.first < y.first; });
+    const size_t top = std::min<size_t>(3, scored.size());
+    for (size_t k = 0; k < top; ++k) {
+        for (int order : {0, 1})
+            for (int spread : {0, 1}) {
+                if (!order && !spread) continue;  // measured in stage 1
+                if (order && n < 2) continue;     // one pair: nothing to order
+                Shape c = scored[k].second;
+                c.order = order;
+                c.spread = spread;
+                double med = 0;
+                const hd_status st = measure(c, &med);
+                if (st != HD_OK) return st;
+                scored.emplace_back(med, c);
+            }
+    }
+    TuneEntry best;
+    best.us = 1e300;
+    for (const auto& sc : scored)
+        if (sc.first < best.us) {
+            best.us = sc.first;
+            best.shape = sc.second;
+        }
     double vox = 0;
     for (const auto& p : in) vox += (double)p.W * p.H * p.D;
     vox /= n;
     const std::string key = tune_key(se, vox, n);
     ctx->tune.entries[key] = best;
-    char line[160];
-    std::snprintf(line, sizeof line, "best %s: kernel=%d bxw=%d bz=%d steps=%d cps=%d %.1f us\n", key.c_str(),
-                  best.shape.kernel, best.shape.bxw, best.shape.bz, best.shape.steps, best.shape.ctas_per_sm, best.us);
+    char line[200];
+    std::snprintf(line, sizeof line, "best %s: kernel=%d bxw=%d bz=%d steps=%d cps=%d order=%d spread=%d %.1f us\n",
+                  key.c_str(), best.shape.kernel, best.shape.bxw, best.shape.bz, best.shape.steps,
+                  best.shape.ctas_per_sm, best.shape.order, best.shape.spread, best.us);
     rep += line;
     if (!ctx->tuning_path.empty() && !ctx->tune.save(ctx->tuning_path))
         set_error(ctx, HD_OK, "autotune: could not write %s", ctx->tuning_path.c_str());

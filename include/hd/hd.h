@@ -177,6 +177,8 @@ hd_status hd_compute_u8_device_async(hd_context* ctx, const uint8_t* d_a, const 
  * previous pair still dilates: single pairs of up to 2^26 voxels on a GPU
  * whose SMs can be split (green contexts) run their packing and set-up on a
  * few SMs and their dilation on the rest, with two workspaces in turn.
+ * `stream` is made to wait for the packing's reads of the masks (not for the
+ * dilation), so work queued on it after the call may overwrite or free them.
  * Otherwise the call behaves like hd_compute_u8_device_async. */
 hd_status hd_compute_u8_device_pipelined(hd_context* ctx, const uint8_t* d_a, const uint8_t* d_b, int32_t W,
                                          int32_t H, int32_t D, hd_metric metric, void* stream, hd_result* d_out);
@@ -225,10 +227,15 @@ hd_status hd_distance_map_device(hd_context* ctx, const uint8_t* d_a, const uint
 
 /* Autotuner (replaces the occupancy-API launch choice of hello.cu:1910-1954):
  * times every compiled brick shape and persistent-grid size on the given
- * pairs (one metric), checks that all give identical results, keeps the
- * fastest for this workload class in the context and, when the context was
- * created with hd_options.tuning_table, writes the table there as JSON.  A
- * human-readable report of the timings goes to `report` (may be NULL). */
+ * pairs (one metric), then the queue schedule (pair order of a batch: as
+ * given or largest first; queue items to warps: CTA-major or spread over the
+ * SMs) on the three fastest; checks that every candidate gives identical
+ * results (every field but `iterations`), keeps the fastest for this
+ * workload class in the context and, when the context was created with
+ * hd_options.tuning_table, writes the table there as JSON (a later context
+ * created with that table uses it).  `repeats` timed runs per candidate
+ * (median).  A human-readable report of the timings goes to `report` (may be
+ * NULL). */
 hd_status hd_autotune(hd_context* ctx, const hd_pair_desc* pairs, int32_t n, int32_t repeats,
                       char* report, size_t report_len);
 
@@ -239,7 +246,9 @@ typedef struct hd_server_options {
     uint64_t hbm_budget_bytes;   /* device bytes the server may hold; 0 = 120 GiB */
     int32_t max_inflight;        /* admitted pairs at once; 0 = unlimited (budget-bound) */
     int32_t max_queue;           /* waiting requests before submit returns HD_ERR_BUSY; 0 = 4096 */
-    int32_t tick_iterations;     /* dilation steps per device tick; 0 = 16 */
+    int32_t tick_iterations;     /* grid-barrier iterations per device tick at most; 0 = 64.  A tick
+                                    also ends when every resident pair has finished, or at its next
+                                    barrier once a request is submitted while it runs */
     int32_t metric;              /* hd_metric of every request of this server */
 } hd_server_options;
 
@@ -253,6 +262,10 @@ hd_status hd_server_submit(hd_server* srv, const hd_pair_desc* pair, uint64_t* t
 hd_status hd_server_poll(hd_server* srv, uint64_t ticket, hd_result* out);
 /* Blocks until the request finishes (timeout_ms < 0: no limit). */
 hd_status hd_server_wait(hd_server* srv, uint64_t ticket, int64_t timeout_ms, hd_result* out);
+/* Blocks until any request finishes (timeout_ms < 0: no limit) and returns
+ * the earliest finished one not yet taken: its ticket and result (the
+ * ticket is then forgotten).  HD_ERR_NOT_READY on timeout. */
+hd_status hd_server_wait_any(hd_server* srv, int64_t timeout_ms, uint64_t* ticket, hd_result* out);
 hd_status hd_server_cancel(hd_server* srv, uint64_t ticket);
 /* Counters: submitted, completed, resident pairs, ticks, device bytes in use. */
 typedef struct hd_server_stats {

@@ -1,7 +1,8 @@
 """The reference's own dilation kernel as a parity pin (test infrastructure).
 
-build() compiles, when the reference sources are present (this container),
-forBench/HausdorffDistance.cu from where it lies under /root/reference to PTX
+build() compiles, when the reference sources are present (the directory named
+by the HD_REFERENCE_ROOT environment variable, else ../reference beside this
+repository), forBench/HausdorffDistance.cu from where it lies to PTX
 twice, once per structuring element the reference's switches select
 (forBench/HausdorffDistance.cuh:7-8):
   oracle/_ref/forbench_se18.ptx  as shipped: IS_3D 1, CHEBYSHEV 1
@@ -28,7 +29,8 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DIR = "/root/reference/forBench"
+REF_ROOT = os.environ.get("HD_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+REF_DIR = os.path.join(REF_ROOT, "forBench")
 REF_SRC = os.path.join(REF_DIR, "HausdorffDistance.cu")
 PTX = {"se18": os.path.join(HERE, "_ref", "forbench_se18.ptx"),
        "se6": os.path.join(HERE, "_ref", "forbench_se6.ptx")}

@@ -49,7 +49,7 @@ def test_options_defaults(hd):
     assert abs(o.percentile - 0.95) < 1e-7 and o.zero_copy == 1 and o.brick_x_words == 0
     s = _native.HdServerOptions()
     _native.load().hd_server_options_init(ctypes.byref(s))
-    assert s.hbm_budget_bytes == 120 << 30 and s.tick_iterations == 16 and s.max_queue == 4096
+    assert s.hbm_budget_bytes == 120 << 30 and s.tick_iterations == 64 and s.max_queue == 4096
 
 
 def test_struct_layouts_match_binding(tmp_path, hd):

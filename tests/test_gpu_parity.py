@@ -469,3 +469,34 @@ def test_async_host_entry_pipelines_copies(hd, ctx):
                 assert g[k] != g[k], (i, k)
             else:
                 assert g[k] == w[k], (i, k, g, w)
+
+
+def test_autotune_table_round_trip(hd, tmp_path):
+    """The autotuner searches shapes and the queue schedule, writes its table,
+    and a new context created with that table runs the tuned shape for the
+    same workload class with the same results."""
+    import json
+    specs = synth.batch_ragged_specs(41, n=20, lo=32, hi=96, edge_frac=0.1)
+    pairs = [synth.pair_from_spec(s, "cuda") for s in specs]
+    path = str(tmp_path / "tune.json")
+    with hd.Context(0, tuning_table=path) as c:
+        rep = c.autotune(pairs, "se6", repeats=3)
+        first = c.batch(pairs, "se6")
+    assert "order=1" in rep and "spread=1" in rep  # the queue schedule was searched
+    best = [ln for ln in rep.splitlines() if ln.startswith("best ")]
+    assert len(best) == 1
+    table = json.load(open(path))["entries"]
+    assert len(table) == 1
+    (key, entry), = table.items()
+    assert best[0].startswith(f"best {key}:")
+    for k in ("kernel", "bz", "steps", "ctas_per_sm", "order", "spread"):
+        assert f"{k if k != 'ctas_per_sm' else 'cps'}={entry[k]}" in best[0]
+    with hd.Context(0, tuning_table=path, record_timings=True) as c2:
+        again = c2.batch(pairs, "se6")
+        t = c2.last_timings()
+    assert t["kernel"] == entry["kernel"] and t["brick_z"] == entry["bz"]
+    if entry["kernel"] == 2:
+        assert t["steps_per_barrier"] == entry["steps"]
+    keys = [k for k in first[0] if k != "iterations"]
+    for x, y in zip(first, again):
+        assert all(x[k] == y[k] or (k == "avg_hd" and x[k] != x[k] and y[k] != y[k]) for k in keys)

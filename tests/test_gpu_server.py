@@ -116,3 +116,22 @@ def test_server_kernels_and_slot_reuse(hd, ctx, opts):
         res = [srv.wait(t, 60000) for t in ts]
     for i, (r, p) in enumerate(zip(res, plain)):
         assert same(r, p), (opts, i, r, p)
+
+
+def test_wait_any_returns_every_request(hd, ctx):
+    """hd_server_wait_any hands out each finished request once, in
+    completion order, with the plain path's result."""
+    pairs = _pairs(20, 29, lo=32, hi=128, edge=0.1)
+    plain = [ctx.compute(a, b, "se6") for a, b in pairs]
+    with hd.Server(ctx) as srv:
+        tickets = {srv.submit(a, b): i for i, (a, b) in enumerate(pairs)}
+        got = {}
+        while len(got) < len(pairs):
+            t, r = srv.wait_any(60000)
+            assert t in tickets and t not in got
+            got[t] = r
+        assert srv.wait_any(10) is None
+    for t, i in tickets.items():
+        assert same(got[t], plain[i]), i
+
+
