@@ -77,11 +77,13 @@ constexpr long long kPackTileWords = 1024;
 // kTbPrefetch planes ahead of the one being computed; a plane stays until
 // its final step has been compared with it, T planes later.  Per warp: the
 // slots (32 rows x (16 B interior + 8 B halo words)) and the brick's
-// target rows (BZ planes x 32 rows x 16 B).  3 CTAs of kTbWarps
-// warps fit on an SM.
+// target rows (BZ planes x 32 rows x 16 B).  CTAs of kTbWarps warps per
+// SM: 3, and 4 for 1 or 2 steps per barrier (registers capped at 128 per
+// thread), whose work per barrier is large enough for more warps to hide
+// the latency of the planes' dependency chains.
 constexpr int kTbWarps = 4;
 constexpr int kTbPrefetch = 2;
-constexpr int kTbMinCtas = 3;
+__host__ __device__ constexpr int tb_min_ctas(int T) { return T <= 2 ? 4 : 3; }
 __host__ __device__ constexpr int tb_ring_slots(int T, int BZ) {
     return T + 1 + kTbPrefetch >= BZ + 2 * T ? BZ + 2 * T : T + 1 + kTbPrefetch;
 }

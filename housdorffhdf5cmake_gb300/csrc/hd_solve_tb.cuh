@@ -521,7 +521,7 @@ __device__ __forceinline__ void tb_epilogue(const SolveParams& p, const TbItem& 
 }
 
 template <int T, int BZ, bool SE18>
-__global__ void __launch_bounds__(kTbWarps * 32, kTbMinCtas) solve_tb_kernel(SolveParams p) {
+__global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel(SolveParams p) {
     extern __shared__ __align__(16) unsigned char tb_smem[];
     __shared__ int s_flag;
     __shared__ unsigned s_gen, s_cnt;
