@@ -268,6 +268,21 @@ def bench_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
 
+    # ---- phases of the launches the value path times --------------------------
+    # the pipelined entry packs on a few SMs and dilates on the rest: CUDA
+    # events on those streams around each kernel (the last of a few
+    # back-to-back calls, whose dilation has no packing beside it; over the
+    # four sequences the last pair alternates between the two pairs)
+    split_ph = []
+    for k in range(4):
+        for j in range(3):
+            x, y = pairs[(k + j) % 2]
+            ctx.compute_pipelined(x, y, "se6", out=outs[j])
+        ctx.flush()
+        torch.cuda.synchronize()
+        tm = ctx.last_timings()
+        if tm["iterations"] == -1:  # the split path ran
+            split_ph.append(tm)
     # ---- roofline of the dominant kernel -------------------------------------
     # algorithmic bytes of the dilation (mean of the two pairs, like the times)
     tiles, bricks = 0, 0
@@ -302,6 +317,21 @@ def bench_ours(args):
             traffic = json.load(f).get("c2_512x512x256_se6", {}).get(kname)
     except Exception:
         traffic = None
+    # the value path's dilation runs on the split SMs when the pipelined
+    # entry split them: its solve time is what the frontier bytes are
+    # divided by; the blocking entry's whole-GPU launch is reported beside it
+    value_launch = None
+    so_whole = so
+    if split_ph and dom == "solve":
+        so_split = statistics.mean(p["solve_ms"] for p in split_ph)
+        value_launch = {
+            "launch": f"solve_tb_kernel on the dilation SMs of the pipelined entry ({split_ph[0]['grid_ctas']} CTAs)",
+            "solve_ms": round(so_split, 4), "pack_ms": round(statistics.mean(p["pack_ms"] for p in split_ph), 4),
+            "setup_ms": round(statistics.mean(p["setup_ms"] for p in split_ph), 4),
+            "achieved": round(b_iter / (so_split * 1e-3) / 1e9, 1)}
+        value_launch["frac"] = round(value_launch["achieved"] / peak, 4)
+        achieved = value_launch["achieved"]
+        so = so_split
     roofline = {
         "bound": "hbm", "kernel": kname + {"solve": " (persistent frontier dilation)", "pack": " (uint8 -> bits)",
                                            "setup": " (crop + first queue)"}[dom],
@@ -313,6 +343,12 @@ def bench_ours(args):
         "solve": {"bytes": b_iter, "ms": round(so, 4), "gbs": round(b_iter / (so * 1e-3) / 1e9, 1),
                   "frontier_tiles": tiles, "bricks_processed": bricks},
     }
+    if value_launch:
+        roofline["value_launch"] = value_launch
+        roofline["whole_gpu_launch"] = {
+            "launch": f"solve_tb_kernel of the blocking entry on every SM ({phases[-1]['grid_ctas']} CTAs)",
+            "solve_ms": round(so_whole, 4), "achieved": round(b_iter / (so_whole * 1e-3) / 1e9, 1),
+            "frac": round(b_iter / (so_whole * 1e-3) / 1e9 / peak, 4)}
     gvox = (refs[0]["hd"] + refs[1]["hd"]) / 2 * 2 * N / (step_ms * 1e-3) / 1e9
 
     out = {
@@ -351,6 +387,9 @@ def bench_ours(args):
         "roofline": roofline, "clocks": clk, "wall_s_timed_region": round(wall, 3),
     }
 
+    if ws > 1 and not args.no_extras:
+        # every rank: the 256-pair ragged batch split over the ranks
+        out["sharded_batch"] = bench_sharded_batch(ctx, args, ws, rank, dist)
     if rank == 0 and ws == 1 and not args.no_extras:
         out["batched"] = bench_batched(ctx, args)
         out["worst_case"] = bench_worst_case(ctx, dev)
@@ -420,9 +459,16 @@ def bench_batched(ctx, args):
             ts.append(e0.elapsed_time(e1))
         return statistics.median(ts)
 
-    reps = max(2, min(args.steps, 3))
-    t_batch = timed(lambda: ctx.batch(pairs, "se6"), reps)
+    reps = max(3, min(args.steps, 5))
+    # the batch call as a loop over the same buffers makes it: descriptors
+    # prepared once, results as numpy columns; the one-shot call (fresh
+    # descriptors, a dict per pair) beside it
+    prep = ctx.prepare_batch(pairs, "se6")
+    cols = prep.run(columns=True)
+    exact = exact and all(int(cols[k][i]) == batch[i][k] for i in range(len(batch)) for k in keys)
+    t_batch = timed(lambda: prep.run(columns=True), reps)
     bt = ctx.last_timings()
+    t_batch_dicts = timed(lambda: ctx.batch(pairs, "se6"), reps)
     t_plain = timed(lambda: [ctx.compute(a, b, "se6") for a, b in pairs], reps)
     # device time alone (CUDA events around the kernels of each call)
     dev_plain = 0.0
@@ -430,10 +476,25 @@ def bench_batched(ctx, args):
         ctx.compute(a, b, "se6")
         dev_plain += ctx.last_timings()["total_ms"]
     gvox = sum(max(0, r["hd"]) * 2 * (s.shape[0] * s.shape[1] * s.shape[2]) for r, s in zip(batch, specs))
+    # roofline of the batch's dilation launch: the frontier bytes of every
+    # pair (32^3 tiles gaining voxels per step, counted by the instrumented
+    # run) over the batch's solve time
+    tiles = 0
+    for (a, b), r in zip(pairs, batch):
+        if r["status"] != 0:
+            continue
+        res, tab, tba, _ = ctx.profile(a, b, "se6")
+        tiles += int(sum(int(v) for v in tab[1: res["hd_ab"] + 1]) + sum(int(v) for v in tba[1: res["hd_ba"] + 1]))
+    b_iter = 3 * 4096 * tiles
+    peak, peak_kind = _peaks()
+    solve_gbs = b_iter / (bt["solve_ms"] * 1e-3) / 1e9
     return {
         "workload": "256 ragged pairs, axes uniform in {64..384}, 5% edge pairs (empty / identical)",
         "pairs": len(pairs), "voxels": voxels,
         "batched_pairs_per_s": round(256 * 1000.0 / t_batch, 2), "batched_ms": round(t_batch, 3),
+        "batched_path": "PreparedBatch.run(columns=True): one hd_batch_compute over descriptors built once",
+        "batched_one_shot_ms": round(t_batch_dicts, 3),
+        "batched_one_shot_path": "Context.batch: descriptors built and one result dict per pair, every call",
         "plain_pairs_per_s": round(256 * 1000.0 / t_plain, 2), "plain_ms": round(t_plain, 3),
         "speedup_batched_vs_plain": round(t_plain / t_batch, 2),
         "device_ms": {"batched": round(bt["total_ms"], 3), "plain_sum": round(dev_plain, 3),
@@ -442,12 +503,52 @@ def bench_batched(ctx, args):
         "batched_phase_ms": {"pack": round(bt["pack_ms"], 3), "setup": round(bt["setup_ms"], 3),
                              "solve": round(bt["solve_ms"], 3), "barrier_iterations": bt["iterations"]},
         "pack_gbs_batched": round((2 * voxels + 2 * voxels / 8) / (bt["pack_ms"] * 1e-3) / 1e9, 1),
+        "solve_roofline": {"bound": "hbm", "algorithmic_bytes": b_iter, "frontier_tiles": tiles,
+                           "solve_ms": round(bt["solve_ms"], 4), "achieved": round(solve_gbs, 1), "peak": peak,
+                           "unit": "GB/s", "frac": round(solve_gbs / peak, 4),
+                           "peak_source": f"{peak_kind} MEASURED_PEAKS hbm_gbs"},
         "bit_exact_vs_plain": bool(exact), "pairs_checked_against_oracle": int(oracle_checked),
         "autotuned": tuned[0] if tuned else None,
         "shape": {"kernel": bt["kernel"], "steps_per_barrier": bt["steps_per_barrier"],
                   "brick_words_rows_planes": [bt["brick_x_words"], bt["brick_rows"], bt["brick_z"]],
                   "grid_ctas": bt["grid_ctas"]},
     }
+
+
+def bench_sharded_batch(ctx, args, ws, rank, dist):
+    """Multi-GPU batches: the 256 ragged pairs split over the ranks
+    largest-first (shard.plan_shards), each rank's share in one persistent
+    launch (ctx.batch), the result records gathered on the host
+    (shard.batch_sharded).  Time: barrier-bracketed, max over ranks."""
+    import torch
+
+    from housdorffhdf5cmake_gb300 import shard, synth
+    specs = synth.batch_ragged_specs(77, n=256)
+    costs = [s.shape[0] * s.shape[1] * s.shape[2] for s in specs]
+    mine = shard.plan_shards(costs, ws)[rank]
+    pairs = [None] * len(specs)
+    for i in mine:  # each rank builds only its own share's masks
+        pairs[i] = synth.pair_from_spec(specs[i], "cuda")
+    torch.cuda.synchronize()
+    run = lambda: shard.batch_sharded(pairs, lambda ps: ctx.batch(ps, "se6"), costs=costs)
+    res = run()  # warm-up (and the check below)
+    ts = []
+    for _ in range(max(2, min(args.steps, 5))):
+        dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        run()
+        torch.cuda.synchronize()
+        dist.barrier()
+        ts.append(time.perf_counter() - t0)
+    t = torch.tensor([statistics.median(ts)], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    checked = sum(_check_fixture(r, "c4", f"pair{i:03d}", "se6", f"sharded batch pair {i}") for i, r in enumerate(res))
+    return {"workload": "256 ragged pairs split over the ranks (largest-first), one batch launch per rank, "
+                        "results gathered on the host",
+            "ranks": ws, "ms": round(float(t.item()) * 1e3, 3),
+            "pairs_per_s": round(len(specs) / float(t.item()), 1),
+            "pairs_on_rank0": len(shard.plan_shards(costs, ws)[0]), "pairs_checked_against_oracle": int(checked)}
 
 
 def bench_serving(ctx, args):
@@ -486,13 +587,14 @@ def bench_serving(ctx, args):
     plain_rate = len(svc) / sum(svc)
     keys = ("hd", "hd_ab", "hd_ba", "sum_ab", "sum_ba", "n_a", "n_b", "status")
 
-    def run(rate):
+    def run(srv, rate):
         stream = synth.serving_stream(77 + int(rate), n=n_req, rate_hz=rate) if rate else None
         arr = [r.t_arrival for r in stream] if stream else [0.0] * n_req
         lat = [None] * n_req
         exact = [True]
         sub = {}  # ticket -> (request index, submit time)
-        with hd.Server(ctx, hbm_budget_bytes=120 << 30) as srv:
+        ticks0 = srv.stats()["ticks"]
+        if True:
             def collect():
                 # hd_server_wait_any: each finished request as soon as the
                 # server completes it, in completion order
@@ -525,6 +627,7 @@ def bench_serving(ctx, args):
             th.join()
             t_end = time.perf_counter()
             st = srv.stats()
+            st["ticks"] -= ticks0
         lat_ms = sorted(x * 1e3 for x in lat)
         # the one-pair-at-a-time path on the same arrivals: FIFO replay
         done, pl = 0.0, []
@@ -543,8 +646,12 @@ def bench_serving(ctx, args):
     switch = sys.getswitchinterval()
     sys.setswitchinterval(2e-5)
     try:
-        rows = [run(f * plain_rate) for f in (0.5, 0.9, 1.5, 3.0)]
-        rows.append(run(0.0))  # every request at t = 0: saturation throughput
+        # one server for every rate, warmed up by a burst of the whole
+        # stream (its memory pool then holds what the timed runs need)
+        with hd.Server(ctx, hbm_budget_bytes=120 << 30) as srv:
+            run(srv, 0.0)
+            rows = [run(srv, f * plain_rate) for f in (0.5, 0.9, 1.5, 3.0)]
+            rows.append(run(srv, 0.0))  # every request at t = 0: saturation throughput
     finally:
         sys.setswitchinterval(switch)
     return {"workload": "open-loop Poisson stream, sizes log-normal around 256x256x160 (cap 512^3, 10% 512^3), "
@@ -680,10 +787,14 @@ def run_case(args):
         else:
             a, b = synth.pair_far_blobs(5, (512, 512, 512), "cuda")
         run = lambda: ctx.compute(a, b, "se6")
+    solves = []
     for _ in range(args.repeat):
         run()
+        solves.append(ctx.last_timings()["solve_ms"])
     torch.cuda.synchronize()
-    print(args.case, json.dumps(ctx.last_timings()), flush=True)
+    t = ctx.last_timings()
+    t["solve_ms_median"] = statistics.median(solves)
+    print(args.case, json.dumps(t), flush=True)
     ctx.close()
 
 

@@ -26,7 +26,7 @@ from ._native import (HD_EMPTY_MASK, HD_ERR_BAD_ARG, HD_ERR_BUSY, HD_ERR_CANCELL
                       HD_ERR_UNSUPPORTED, HD_OK, HD_SE6, HD_SE18_FORBENCH)
 
 __all__ = [
-    "Context", "Server", "HausdorffDistance", "Volume", "HDError", "metric_code", "load_hdf5_bool",
+    "Context", "PreparedBatch", "Server", "HausdorffDistance", "Volume", "HDError", "metric_code", "load_hdf5_bool",
     "HD_OK", "HD_EMPTY_MASK", "HD_ERR_BAD_ARG", "HD_ERR_OOM", "HD_ERR_CUDA", "HD_ERR_TIMEOUT",
     "HD_ERR_CANCELLED", "HD_ERR_ITER_LIMIT", "HD_ERR_NOT_READY", "HD_ERR_UNSUPPORTED", "HD_ERR_BUSY",
     "HD_SE6", "HD_SE18_FORBENCH",
@@ -62,23 +62,6 @@ def _dims(x):
 
 
 _torch = None
-
-
-def _fast_cuda(x):
-    """(pointer, W, H, D) of a contiguous 3-D uint8 CUDA tensor, else None
-    (a handful of attribute reads: batches touch hundreds of tensors)."""
-    global _torch
-    if _torch is None:
-        if not type(x).__module__.startswith("torch"):
-            return None
-        import torch
-        _torch = torch
-    if type(x) is not _torch.Tensor or x.dtype is not _torch.uint8 or not x.is_cuda or not x.is_contiguous():
-        return None
-    sh = x.shape
-    if len(sh) != 3:
-        return None
-    return (x.data_ptr(), sh[2], sh[1], sh[0])
 
 
 _PAIR_DESC_DTYPE = np.dtype({
@@ -321,53 +304,17 @@ class Context:
 
     # -- batches --------------------------------------------------------------
     def batch(self, pairs: Sequence, metric="se6") -> list:
-        """One hd_batch_compute over [(a, b), ...] (host or CUDA masks).
-        The descriptor array is filled column-wise through numpy (per-field
-        ctypes writes would cost more than the device work of small pairs)."""
-        n = len(pairs)
-        if n == 0:
+        """One hd_batch_compute over [(a, b), ...] (host or CUDA masks): one
+        result dict per pair, in order."""
+        if len(pairs) == 0:
             return []
-        keep, rows = [], []
-        any_dev = False
-        global _torch
-        if _torch is None:
-            try:
-                import torch
-                _torch = torch
-            except ImportError:
-                pass
-        T = _torch.Tensor if _torch is not None else None
-        u8 = _torch.uint8 if _torch is not None else None
-        for i, (a, b) in enumerate(pairs):
-            # contiguous 3-D uint8 CUDA tensors: a handful of attribute reads
-            # inline (batches touch hundreds of tensors); anything else
-            # through _Buf
-            if (type(a) is T and type(b) is T and a.dtype is u8 and b.dtype is u8 and a.is_cuda and b.is_cuda
-                    and a.is_contiguous() and b.is_contiguous()):
-                sh = a.shape
-                if len(sh) == 3 and sh == b.shape:
-                    rows.append((a.data_ptr(), b.data_ptr(), sh[2], sh[1], sh[0], 1))
-                    any_dev = True
-                    continue
-            A, B = _Buf(a), _Buf(b)
-            if (A.W, A.H, A.D) != (B.W, B.H, B.D) or A.on_device != B.on_device:
-                raise ValueError(f"pair {i}: shapes or devices differ")
-            keep.append((A, B))
-            any_dev = any_dev or A.on_device
-            rows.append((A.ptr, B.ptr, A.W, A.H, A.D, 1 if A.on_device else 0))
-        descs = np.zeros(n, dtype=_PAIR_DESC_DTYPE)
-        cols = np.array(rows, dtype=np.int64).T
-        descs["a"], descs["b"] = cols[0], cols[1]
-        descs["W"], descs["H"], descs["D"] = cols[2], cols[3], cols[4]
-        descs["metric"] = metric_code(metric)
-        descs["on_device"] = cols[5]
-        res = (N.HdResult * n)()
-        if any_dev:
-            import torch
-            torch.cuda.current_stream().synchronize()  # this call runs on the context's stream
-        code = N.load().hd_batch_compute(self._h, descs.ctypes.data_as(ctypes.POINTER(N.HdPairDesc)), n, res)
-        _check(code, self._h)
-        return _result_dicts(res, n)
+        return self.prepare_batch(pairs, metric).run()
+
+    def prepare_batch(self, pairs: Sequence, metric="se6") -> "PreparedBatch":
+        """The descriptor array of a batch, built once for repeated runs over
+        the same mask buffers (an evaluation or serving loop that refills
+        them between runs); see PreparedBatch."""
+        return PreparedBatch(self, pairs, metric)
 
     # -- instrumentation --------------------------------------------------------
     def profile(self, a, b, metric="se6"):
@@ -406,6 +353,17 @@ class Context:
         _check(code, self._h)
         return r.as_dict(), ma, mb
 
+    def compute_hdf5(self, path_a: str, dataset_a: str, path_b: str, dataset_b: str, shape, metric="se6") -> dict:
+        """The reference's HDF5 host path for one pair (hd_compute_hdf5):
+        two flat boolean datasets of D*H*W elements, x fastest; shape =
+        (D, H, W)."""
+        D, H, W = (int(v) for v in shape)
+        r = N.HdResult()
+        code = N.load().hd_compute_hdf5(self._h, path_a.encode(), dataset_a.encode(), path_b.encode(),
+                                        dataset_b.encode(), W, H, D, metric_code(metric), ctypes.byref(r))
+        _check(code, self._h)
+        return r.as_dict()
+
     def autotune(self, pairs: Sequence, metric="se6", repeats: int = 3) -> str:
         n = len(pairs)
         bufs = []
@@ -422,6 +380,75 @@ class Context:
         code = N.load().hd_autotune(self._h, descs, n, int(repeats), rep, len(rep))
         _check(code, self._h, allow_empty=False)
         return rep.value.decode()
+
+
+class PreparedBatch:
+    """A batch whose descriptor array (mask pointers and sizes, filled
+    column-wise through numpy) is built once; run() makes one
+    hd_batch_compute call over it.  The masks must stay allocated (and
+    their pointers unchanged) while the batch is in use; their contents may
+    change between runs."""
+
+    def __init__(self, ctx: "Context", pairs: Sequence, metric="se6"):
+        n = len(pairs)
+        keep, rows = [], []
+        any_dev = False
+        global _torch
+        if _torch is None:
+            try:
+                import torch
+                _torch = torch
+            except ImportError:
+                pass
+        T = _torch.Tensor if _torch is not None else None
+        u8 = _torch.uint8 if _torch is not None else None
+        for i, (a, b) in enumerate(pairs):
+            # contiguous 3-D uint8 CUDA tensors: a handful of attribute reads
+            # inline (batches touch hundreds of tensors); anything else
+            # through _Buf
+            if (type(a) is T and type(b) is T and a.dtype is u8 and b.dtype is u8 and a.is_cuda and b.is_cuda
+                    and a.is_contiguous() and b.is_contiguous()):
+                sh = a.shape
+                if len(sh) == 3 and sh == b.shape:
+                    keep.append((a, b))
+                    rows.append((a.data_ptr(), b.data_ptr(), sh[2], sh[1], sh[0], 1))
+                    any_dev = True
+                    continue
+            A, B = _Buf(a), _Buf(b)
+            if (A.W, A.H, A.D) != (B.W, B.H, B.D) or A.on_device != B.on_device:
+                raise ValueError(f"pair {i}: shapes or devices differ")
+            keep.append((A, B))
+            any_dev = any_dev or A.on_device
+            rows.append((A.ptr, B.ptr, A.W, A.H, A.D, 1 if A.on_device else 0))
+        descs = np.zeros(n, dtype=_PAIR_DESC_DTYPE)
+        if n:
+            cols = np.array(rows, dtype=np.int64).T
+            descs["a"], descs["b"] = cols[0], cols[1]
+            descs["W"], descs["H"], descs["D"] = cols[2], cols[3], cols[4]
+            descs["metric"] = metric_code(metric)
+            descs["on_device"] = cols[5]
+        self._ctx, self._keep, self._descs, self._n, self._dev = ctx, keep, descs, n, any_dev
+        self._ptr = descs.ctypes.data_as(ctypes.POINTER(N.HdPairDesc))
+        self._res = (N.HdResult * max(n, 1))()
+
+    def __len__(self):
+        return self._n
+
+    def run(self, columns: bool = False):
+        """Computes every pair.  Returns one result dict per pair, or with
+        columns=True one numpy array per result field (hd, sum_ab, ...,
+        avg_hd; pair i at index i), which skips building a dict per pair."""
+        n = self._n
+        if n == 0:
+            return {f: np.zeros(0, _RESULT_DTYPE[f]) for f in _RESULT_FIELDS} if columns else []
+        if self._dev:
+            _torch.cuda.current_stream().synchronize()  # this call runs on the context's stream
+        code = N.load().hd_batch_compute(self._ctx._h, self._ptr, n, self._res)
+        _check(code, self._ctx._h)
+        if columns:
+            arr = np.frombuffer(self._res, dtype=_RESULT_DTYPE, count=n)
+            return {f: arr[f].copy() for f in _RESULT_FIELDS}
+        return _result_dicts(self._res, n)
 
 
 class Server:

@@ -35,7 +35,8 @@ EXPORTS = (
     "hd_profile_u8_device", "hd_distance_map_device", "hd_autotune", "hd_server_options_init",
     "hd_server_create", "hd_server_submit", "hd_server_poll", "hd_server_wait", "hd_server_wait_any",
     "hd_server_cancel",
-    "hd_server_get_stats", "hd_server_destroy", "hd_compute_u8_device_noalloc", "hd_load_hdf5_bool", "hd_free",
+    "hd_server_get_stats", "hd_server_destroy", "hd_compute_u8_device_noalloc", "hd_load_hdf5_bool", "hd_compute_hdf5",
+    "hd_free",
 )
 
 
@@ -189,6 +190,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             "hd_compute_u8_device_noalloc": (st, [vp, vp, i32, i32, i32, st, vp, vp]),
             "hd_load_hdf5_bool": (st, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(vp),
                                        ctypes.POINTER(ctypes.c_size_t)]),
+            "hd_compute_hdf5": (st, [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                                     ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int, res_p]),
             "hd_free": (None, [vp]),
         }
         for name, (restype, argtypes) in sig.items():

@@ -43,7 +43,7 @@ def _headers():
 
 
 def _compile(src: str, newest_header: float, extra) -> str:
-    obj = os.path.join(OBJ, os.path.basename(src) + ".o")
+    obj = os.path.join(OBJ, os.path.basename(src) + (".hdf5.o" if "-DHD_WITH_HDF5" in extra else ".o"))
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), newest_header):
         return obj
     tmp = obj + f".tmp{os.getpid()}"
@@ -56,20 +56,32 @@ def _compile(src: str, newest_header: float, extra) -> str:
 
 
 def build(verbose: bool = False, extra_flags=None) -> str:
-    """Compile and link the library; returns the path of the .so."""
+    """Compile and link the library; returns the path of the .so.
+
+    HD_WITH_HDF5=1 in the environment compiles the HDF5 entry points against
+    HDF5's C library (hdf5.h on the include path, -lhdf5 at the link)."""
     os.makedirs(OBJ, exist_ok=True)
     extra = list(extra_flags or [])
+    libs = []
+    if os.environ.get("HD_WITH_HDF5") == "1":
+        extra.append("-DHD_WITH_HDF5")
+        libs.append("-lhdf5")
     srcs = _sources()
     newest = max(os.path.getmtime(h) for h in _headers() + [os.path.abspath(__file__)])
     with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, newest, extra), srcs))
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
+    stamp = os.path.join(BUILD, "link_inputs.txt")  # relink when the object set changes (HDF5 on / off)
+    inputs = "\n".join(objs + libs)
+    same = os.path.exists(stamp) and open(stamp).read() == inputs
+    if not same or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
         tmp = LIB + f".tmp{os.getpid()}"
-        cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs, "-lpthread", "-ldl", "-lrt"]
+        cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs, *libs, "-lpthread", "-ldl", "-lrt"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+        with open(stamp, "w") as f:
+            f.write(inputs)
     if verbose:
         print(LIB)
     return LIB

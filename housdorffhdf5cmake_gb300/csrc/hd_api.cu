@@ -235,6 +235,8 @@ bool split_ready(hd_context* ctx) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sp.caller, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sp.prep_done, cudaEventDisableTiming);
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&sp.ws_free[i], cudaEventDisableTiming);
+    if (ctx->opt.record_timings)
+        for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&sp.ev[i]);
     sp.green[0] = g[0];
     sp.green[1] = g[1];
     sp.solve = (cudaStream_t)st[0];
@@ -258,7 +260,8 @@ void split_release(hd_context* ctx) {
             cudaStreamSynchronize(s);
             cudaStreamDestroy(s);
         }
-    for (cudaEvent_t ev : {sp.caller, sp.prep_done, sp.ws_free[0], sp.ws_free[1]})
+    for (cudaEvent_t ev : {sp.caller, sp.prep_done, sp.ws_free[0], sp.ws_free[1], sp.ev[0], sp.ev[1], sp.ev[2],
+                           sp.ev[3], sp.ev[4]})
         if (ev) cudaEventDestroy(ev);
     auto destroy = driver_fn<GreenDestroyFn>("cuGreenCtxDestroy", 12040);
     for (void* g : sp.green)
@@ -637,6 +640,9 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     const PairDesc* ddesc = (const PairDesc*)(dbase + off_descs);
     const bool timing = ctx->opt.record_timings != 0 && ctx->ev[0] != nullptr && !async;
     if (timing) cudaEventRecord(ctx->ev[0], s);
+    // the split path times its phases on the streams they run on
+    const bool stime = split && ctx->opt.record_timings != 0 && ctx->split.ev[0] != nullptr;
+    if (stime) cudaEventRecord(ctx->split.ev[0], sq);
     e = hdk::launch_pack(ddesc, n, pack_tiles, grid_pack, ctx->opt.label, split ? prep_sms : 0, sq);
     if (e == cudaSuccess && mb >= 0) e = cudaEventRecord(ctx->mask_free[mb], sq);  // staging buffer read
     if (e != cudaSuccess) return cuda_fail(ctx, e, "pack launch");
@@ -647,12 +653,14 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
                                  (unsigned long long*)(dbase + off_q[1]),
                                  (unsigned long long*)(dbase + off_q[2])};
     if (timing) cudaEventRecord(ctx->ev[1], s);
+    if (stime) cudaEventRecord(ctx->split.ev[1], sq);
     e = hdk::launch_setup(ddesc, n, setup_tiles, grid_setup, djobs, dstates, dq[g0 % 3], dctl, g0, bxw, by, bz,
                           setup_mode, sq);
     if (e == cudaSuccess && split) {
         // the dilation follows the set-up; the caller's stream follows the
         // packing's reads of its masks (work it queues later may overwrite
         // or free them) but not the dilation
+        if (stime) cudaEventRecord(ctx->split.ev[2], sq);
         e = cudaEventRecord(ctx->split.prep_done, sq);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(sv, ctx->split.prep_done, 0);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ctx->split.prep_done, 0);
@@ -694,7 +702,19 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     sp.out = async ? ro.async_out : (hd_result*)(dbase + off_out);
     void* args[] = {&sp};
     if (timing) cudaEventRecord(ctx->ev[2], s);
+    if (stime) cudaEventRecord(ctx->split.ev[3], sv);  // after the previous dilation and this set-up
     e = cudaLaunchCooperativeKernel(solve_fn, grid, block, args, (size_t)sh.smem, sv);
+    if (e == cudaSuccess && stime) {
+        cudaEventRecord(ctx->split.ev[4], sv);
+        ctx->split.timed = true;
+        hd_timings& T = ctx->split.shape;
+        T.grid_ctas = (int)grid.x;
+        T.brick_x_words = bxw;
+        T.brick_z = bz;
+        T.kernel = sh.kernel;
+        T.steps_per_barrier = sh.steps;
+        T.brick_rows = by;
+    }
     if (e == cudaSuccess && split) {
         e = cudaEventRecord(ctx->split.ws_free[ws], sv);
         ctx->split.pending = true;
@@ -733,6 +753,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     const Ctl* hctl = (const Ctl*)(hbase + off_ctl);
     ctx->g_next = std::max(ctx->g_next, hctl->g_end) + 2;
     if (timing) {
+        ctx->split.timed = false;
         hd_timings& T = ctx->last_timings;
         cudaEventElapsedTime(&T.pack_ms, ctx->ev[0], ctx->ev[1]);
         cudaEventElapsedTime(&T.setup_ms, ctx->ev[1], ctx->ev[2]);
@@ -898,6 +919,22 @@ const char* hd_context_last_error(hd_context* ctx) { return ctx ? ctx->last_erro
 hd_status hd_context_last_timings(hd_context* ctx, hd_timings* out) {
     if (!ctx || !out) return HD_ERR_BAD_ARG;
     std::lock_guard<std::mutex> lk(ctx->mu);
+    if (ctx->split.timed) {
+        // the latest pipelined call on split SMs: its phases once complete
+        DeviceGuard g(ctx->device);
+        if (cudaEventQuery(ctx->split.ev[4]) != cudaSuccess) {
+            cudaGetLastError();
+            return HD_ERR_NOT_READY;
+        }
+        hd_timings T = ctx->split.shape;
+        cudaEventElapsedTime(&T.pack_ms, ctx->split.ev[0], ctx->split.ev[1]);
+        cudaEventElapsedTime(&T.setup_ms, ctx->split.ev[1], ctx->split.ev[2]);
+        cudaEventElapsedTime(&T.solve_ms, ctx->split.ev[3], ctx->split.ev[4]);
+        cudaEventElapsedTime(&T.total_ms, ctx->split.ev[0], ctx->split.ev[4]);
+        T.iterations = -1;  // not read back by the enqueue-only entry
+        ctx->split.timed = false;
+        ctx->last_timings = T;
+    }
     *out = ctx->last_timings;
     return HD_OK;
 }

@@ -133,6 +133,13 @@ struct hd_context {
         int next = 0;
         bool pending = false;  // a dilation the caller's stream has not waited for yet
         int last = 0;          // the workspace of the latest dilation
+        // record_timings: events of the latest call on the split SMs, each on
+        // the stream its kernel ran on (before pack, after pack, after
+        // set-up; before and after the dilation); read by
+        // hd_context_last_timings once they have completed
+        cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+        bool timed = false;
+        hd_timings shape{};  // the fields of hd_timings that are not times
     } split;
     hdh::DeviceArena arena2;  // the split path's second workspace
 };

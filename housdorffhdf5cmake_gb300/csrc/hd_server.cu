@@ -98,6 +98,10 @@ struct RangeAlloc {
 
 inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
+// How long the scheduler polls for new requests when it runs out of work
+// before it sleeps on the condition variable.
+constexpr int kIdleSpinUs = 500;
+
 }  // namespace
 
 struct hd_server {
@@ -249,21 +253,32 @@ void tick(hd_server* s) {
     cudaStream_t st = s->stream;
     cudaError_t e = cudaSuccess;
     // ---- admission: allocate, upload, pack, set up --------------------------
-    std::vector<void*> transient(admit.size(), nullptr);
     std::vector<PairDesc> descs;
     std::vector<Request*> admitted;
     long long ptiles = 0, stiles = 0;
     // the packed masks are freed after set-up: the blocked kernel reads crops
     const int setup_mode = s->shape.kernel == 1 ? hdk::kSetupOneStep : hdk::kSetupBlockedCrop;
+    // the admitted pairs' transient buffers (packed masks, staged host masks)
+    // in one block for the tick, freed after the set-up; a block per pair
+    // for what lives until the pair completes
+    size_t transient_total = 0;
+    for (Request* r : admit) transient_total += align_up(r->transient_bytes);
+    void* tblock = nullptr;
+    if (transient_total) {
+        e = cudaMallocFromPoolAsync(&tblock, transient_total, s->pool, st);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            tblock = nullptr;
+        }
+    }
+    size_t toff = 0;
     for (size_t i = 0; i < admit.size(); ++i) {
         Request* r = admit[i];
         void* res = nullptr;
-        void* tr = nullptr;
-        e = cudaMallocFromPoolAsync(&res, r->resident_bytes, s->pool, st);
-        if (e == cudaSuccess) e = cudaMallocFromPoolAsync(&tr, r->transient_bytes, s->pool, st);
-        if (e != cudaSuccess) {
+        if (tblock) e = cudaMallocFromPoolAsync(&res, r->resident_bytes, s->pool, st);
+        if (!tblock || e != cudaSuccess) {
             cudaGetLastError();
-            if (res) cudaFreeAsync(res, st);
+            e = cudaSuccess;
             std::lock_guard<std::mutex> lk(s->mu);
             s->stats.bytes_in_use -= r->resident_bytes + r->transient_bytes;
             s->bricks.release(r->brick0, 2 * r->nbricks);
@@ -273,9 +288,9 @@ void tick(hd_server* s) {
             continue;
         }
         r->resident = res;
-        transient[i] = tr;
         char* rb = (char*)res;
-        char* tb = (char*)tr;
+        char* tb = (char*)tblock + toff;
+        toff += align_up(r->transient_bytes);
         const size_t nb = (size_t)r->W * r->H * r->D;
         const size_t packed = align_up(4ULL * hdk::packed_pitch(r->W) * r->H * r->D);
         PairDesc d{};
@@ -338,8 +353,7 @@ void tick(hd_server* s) {
             cuda_err(s, e, "admission");
         }
     }
-    for (void* tr : transient)
-        if (tr) cudaFreeAsync(tr, st);
+    if (tblock) cudaFreeAsync(tblock, st);
     {
         std::lock_guard<std::mutex> lk(s->mu);
         for (auto* r : admitted) s->stats.bytes_in_use -= r->transient_bytes;
@@ -475,6 +489,10 @@ void tick(hd_server* s) {
             complete(s, r, st_r);
         }
     }
+    if (!finished.empty()) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->done_cv.notify_all();  // results first, clean-up after
+    }
     if (nretire) {
         // the list is read before the next tick rewrites it (the end of
         // every tick waits for the stream)
@@ -514,16 +532,26 @@ void tick(hd_server* s) {
 
 void worker_main(hd_server* s) {
     DeviceGuard g(s->ctx->device);
+    auto has_work = [&] {
+        if (s->stop) return true;
+        if (!s->waiting.empty()) return true;
+        for (auto* r : s->slots)
+            if (r) return true;
+        return false;
+    };
     for (;;) {
+        // idle: poll for a new request for a short while before sleeping
+        // (a wake-up through the condition variable costs tens of
+        // microseconds of a request's latency)
+        const auto t_idle = std::chrono::steady_clock::now();
+        bool work = false;
+        while (!work && std::chrono::steady_clock::now() - t_idle < std::chrono::microseconds(kIdleSpinUs)) {
+            std::lock_guard<std::mutex> lk(s->mu);
+            work = has_work();
+        }
         {
             std::unique_lock<std::mutex> lk(s->mu);
-            s->cv.wait(lk, [&] {
-                if (s->stop) return true;
-                if (!s->waiting.empty()) return true;
-                for (auto* r : s->slots)
-                    if (r) return true;
-                return false;
-            });
+            s->cv.wait(lk, has_work);
             if (s->stop) return;
         }
         tick(s);

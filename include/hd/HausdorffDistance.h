@@ -57,6 +57,21 @@ public:
     /* Full result of the last kind (status, sums, counts, robust HD). */
     hd_status computeResult(Volume* img1, Volume* img2, hd_result* out) { return run(img1, img2, out); }
 
+    /* The reference's HDF5 host path (loadHDF -> loadHDFIntoBoolArr x 2 ->
+     * Volumes -> computeDistance, forBench/hdf5Manag.cu:196-214, 93-111):
+     * max HD of two flat boolean datasets of width x height x depth
+     * elements, or -1 on error (missing file or dataset, size mismatch, a
+     * library built without HDF5, one empty mask). */
+    int computeDistanceHdf5(const char* pathA, const char* datasetA, const char* pathB, const char* datasetB,
+                            int width, int height, int depth) {
+        hd_context* ctx = context();
+        if (!ctx) return -1;
+        hd_result r;
+        return hd_compute_hdf5(ctx, pathA, datasetA, pathB, datasetB, width, height, depth, metric_, &r) == HD_OK
+                   ? r.hd
+                   : -1;
+    }
+
 private:
     static hd_context* context() {
         static hd_context* ctx = [] {

@@ -131,7 +131,9 @@ hd_status hd_context_destroy(hd_context* ctx);
 /* Text of the last error seen by this context ("" if none). */
 const char* hd_context_last_error(hd_context* ctx);
 /* Kernel timings of the context's last pair computation (zeros unless the
- * context was created with record_timings = 1). */
+ * context was created with record_timings = 1).  After a pipelined call on
+ * split SMs: its packing and set-up on their SMs and its dilation on the
+ * others (iterations -1), HD_ERR_NOT_READY until that dilation is done. */
 hd_status hd_context_last_timings(hd_context* ctx, hd_timings* out);
 
 /* Drop-in for HausdorffDistance::computeDistance (forBench/HausdorffDistance.cu:101):
@@ -296,9 +298,17 @@ hd_status hd_compute_u8_device_noalloc(const uint8_t* d_a, const uint8_t* d_b, i
                                        int32_t D, hd_metric metric, void* stream, hd_result* d_out);
 
 /* ---- HDF5 input (forBench/hdf5Manag.cu:44-86, loadHDFIntoBoolArr) -------- */
-/* Reads a rank-1 boolean dataset into a malloc'd byte array.  Returns
- * HD_ERR_UNSUPPORTED when the library was built without HDF5. */
+/* Reads a boolean dataset (read as HDF5's native boolean, narrowed to one
+ * byte per element, nonzero = 1) into a malloc'd byte array; *n = elements.
+ * Returns HD_ERR_UNSUPPORTED when the library was built without HDF5. */
 hd_status hd_load_hdf5_bool(const char* path, const char* dataset, uint8_t** out, size_t* n);
+/* The reference's host path for one pair (loadHDF -> loadHDFIntoBoolArr x 2
+ * -> Volumes -> computeDistance, forBench/hdf5Manag.cu:196-214, 93-111):
+ * loads two flat boolean datasets of W*H*D elements (x fastest) and computes
+ * the pair with hd_compute_u8.  HD_ERR_BAD_ARG when a dataset is missing or
+ * its size differs from W*H*D; HD_ERR_UNSUPPORTED without HDF5. */
+hd_status hd_compute_hdf5(hd_context* ctx, const char* path_a, const char* dataset_a, const char* path_b,
+                          const char* dataset_b, int32_t W, int32_t H, int32_t D, hd_metric metric, hd_result* out);
 void hd_free(void* p);
 
 #ifdef __cplusplus

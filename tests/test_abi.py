@@ -86,6 +86,16 @@ def test_hdf5_loader_reports_unsupported(hd):
     assert ei.value.code in (hd.HD_ERR_UNSUPPORTED, hd.HD_ERR_BAD_ARG)
 
 
+def test_hdf5_pair_entry_without_hdf5(hd):
+    """hd_compute_hdf5 answers HD_ERR_UNSUPPORTED in a build without HDF5 (no
+    GPU touched); with HDF5 it validates its arguments first."""
+    from housdorffhdf5cmake_gb300 import _native as N
+    r = N.HdResult()
+    code = N.load().hd_compute_hdf5(None, b"/nonexistent.h5", b"a", b"/nonexistent.h5", b"b", 4, 4, 4, 0,
+                                    ctypes.byref(r))
+    assert code in (hd.HD_ERR_UNSUPPORTED, hd.HD_ERR_BAD_ARG)
+
+
 def test_context_without_gpu_fails_cleanly(hd):
     import torch
     if torch.cuda.is_available():

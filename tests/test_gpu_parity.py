@@ -500,3 +500,19 @@ def test_autotune_table_round_trip(hd, tmp_path):
     keys = [k for k in first[0] if k != "iterations"]
     for x, y in zip(first, again):
         assert all(x[k] == y[k] or (k == "avg_hd" and x[k] != x[k] and y[k] != y[k]) for k in keys)
+
+
+def test_prepared_batch_columns_equal_batch(hd, ctx):
+    """A prepared batch run twice (columns and dicts) equals batch()."""
+    specs = synth.batch_ragged_specs(43, n=12, lo=24, hi=80, edge_frac=0.2)
+    pairs = [synth.pair_from_spec(s, "cuda") for s in specs]
+    want = ctx.batch(pairs, "se6")
+    prep = ctx.prepare_batch(pairs, "se6")
+    assert len(prep) == 12
+    for _ in range(2):
+        cols = prep.run(columns=True)
+        got = prep.run()
+        for i, w in enumerate(want):
+            for k in KEYS:
+                assert got[i][k] == w[k] and int(cols[k][i]) == w[k], (i, k)
+    assert ctx.prepare_batch([], "se6").run(columns=True)["hd"].shape == (0,)

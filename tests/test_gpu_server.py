@@ -135,3 +135,27 @@ def test_wait_any_returns_every_request(hd, ctx):
         assert same(got[t], plain[i]), i
 
 
+
+
+def test_arrival_joins_a_running_tick(hd, ctx):
+    """Continuous batching: a request submitted while a long tick runs (the
+    512^3 far-blobs pair, hundreds of steps, ticks long enough to finish it
+    in one) ends that tick at its next grid barrier and is admitted beside
+    the big pair while the big pair still dilates (two pairs resident at
+    once); both results equal the plain path."""
+    big = synth.pair_far_blobs(5, (512, 512, 512), "cuda")
+    small = _pairs(1, 31, lo=48, hi=64, edge=0.0)[0]
+    want_big, want_small = ctx.compute(*big, "se6"), ctx.compute(*small, "se6")
+    with hd.Server(ctx, tick_iterations=100000) as srv:
+        tb = srv.submit(*big)
+        t0 = time.time()
+        while srv.stats()["resident_pairs"] == 0 and time.time() - t0 < 10:
+            time.sleep(0.0002)
+        time.sleep(0.001)  # the big pair's tick is running now
+        ts = srv.submit(*small)
+        most = 0
+        while srv.stats()["completed"] == 0 and time.time() - t0 < 30:
+            most = max(most, srv.stats()["resident_pairs"])
+        got = dict([srv.wait_any(60000), srv.wait_any(60000)])
+    assert most == 2, "the second pair was not admitted while the first one ran"
+    assert same(got[ts], want_small) and same(got[tb], want_big)

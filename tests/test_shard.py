@@ -117,3 +117,54 @@ def test_two_gloo_ranks_gather_every_result_in_order(oracle):
 def test_without_process_group_runs_locally():
     pairs = _pairs()[:3]
     assert _same(batch_sharded(pairs, _oracle_batch), _oracle_batch(pairs))
+
+
+def _library_shaped_batch(pairs):
+    """A compute with the library's result records: the fields of hd_result
+    (housdorffhdf5cmake_gb300._native.HdResult), filled from the oracle."""
+    from housdorffhdf5cmake_gb300 import _native as N
+    from oracle import oracle as O
+    out = []
+    for a, b in pairs:
+        o = O.forbench(a, b, "se6")
+        r = N.HdResult()
+        for f, _ in N.HdResult._fields_:
+            if f in o:
+                setattr(r, f, o[f])
+        out.append(r.as_dict())
+    return out
+
+
+def _rank_library_records(rank, ws, port, q):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    try:
+        res = batch_sharded(_pairs(), _library_shaped_batch)
+        q.put((rank, res))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_sharded_gather_of_library_records_world2():
+    """batch_sharded over two gloo ranks with a compute that returns the
+    library's result records (what ctx.batch returns): every pair's record,
+    in input order, equal to the whole batch in one process."""
+    want = _library_shaped_batch(_pairs())
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    procs = [ctx.Process(target=_rank_library_records, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = dict(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for r in (0, 1):
+        assert len(got[r]) == len(want)
+        for x, y in zip(got[r], want):
+            assert set(x) == set(y)
+            assert all(x[k] == y[k] or (x[k] != x[k] and y[k] != y[k]) for k in x)
