@@ -344,6 +344,8 @@ def bench_ours(args):
                   "frontier_tiles": tiles, "bricks_processed": bricks},
     }
     if value_launch:
+        roofline["traffic_source"] = ("ncu capture of the same kernel on every SM (bench.py --case c2): ncu cannot "
+                                      "profile kernels launched in a green context")
         roofline["value_launch"] = value_launch
         roofline["whole_gpu_launch"] = {
             "launch": f"solve_tb_kernel of the blocking entry on every SM ({phases[-1]['grid_ctas']} CTAs)",

@@ -99,8 +99,15 @@ struct RangeAlloc {
 inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
 // How long the scheduler polls for new requests when it runs out of work
-// before it sleeps on the condition variable.
+// before it sleeps on the condition variable, and how long hd_server_wait /
+// hd_server_wait_any poll before they sleep.
 constexpr int kIdleSpinUs = 500;
+constexpr int kWaitSpinUs = 200;
+// Busy periods: single-pair kernel shape when at most kFewRequests wait as
+// the server starts work; batch shape after a drain once more than
+// kQueueForBatchMode wait.
+constexpr int kFewRequests = 2;
+constexpr int kQueueForBatchMode = 8;
 
 }  // namespace
 
@@ -108,6 +115,18 @@ struct hd_server {
     hd_context* ctx = nullptr;
     hd_server_options opt{};
     int se = 0, grid = 0;
+    // The dilation kernel's shape, chosen per busy period (the server is
+    // empty when it changes: bricks of one shape cannot continue under
+    // another): modes[0] the single-pair shape (more steps per barrier,
+    // fewer barriers for a lone request), modes[1] the batch shape; `mode`
+    // selects, and shape / solve_fn / grid are the selected mode's.
+    struct Mode {
+        Shape shape;
+        const void* fn = nullptr;
+        int grid = 0;
+    } modes[2];
+    int mode = 1;
+    bool draining = false;  // single-pair mode with a queue building up: admit nothing until empty
     Shape shape;
     const void* solve_fn = nullptr;
     cudaStream_t stream = nullptr;
@@ -167,11 +186,9 @@ hd_status cuda_err(hd_server* s, cudaError_t e, const char* where) {
 // the blocked kernel), histograms, counts.  Transient: the packed masks and
 // the staged host masks.
 void plan_request(hd_server* s, Request* r) {
-    const int by = s->shape.by;
     r->wxf = (r->W + 31) / 32;
     const long long pitch = (r->wxf + 3) / 4 * 4;
     r->dom_words = pitch * r->H * r->D;
-    r->nbricks = (unsigned long long)hdk::bricks_max(r->W, r->H, r->D, s->shape.bxw, by, s->shape.bz);
     r->kmax = r->W + r->H + r->D;
     const size_t job_bytes = align_up(4ULL * r->dom_words);
     r->off_hist = 6 * job_bytes;
@@ -219,7 +236,23 @@ void tick(hd_server* s) {
         }
         for (int q : s->quarantine) s->free_slots.push_back(q);
         s->quarantine.clear();
-        while (!s->waiting.empty() && (int)admit.size() < s->max_admit && !s->free_slots.empty()) {
+        // Kernel shape per busy period: a server that starts work with few
+        // requests waiting takes the single-pair shape; once requests queue
+        // up behind it, it admits nothing until the resident pairs are done
+        // and then takes the batch shape.
+        bool any_resident = false;
+        for (auto* r : s->slots) any_resident = any_resident || r != nullptr;
+        if (!any_resident && !s->waiting.empty()) {
+            const int want = s->waiting.size() <= (size_t)kFewRequests ? 0 : 1;
+            s->mode = want;
+            s->shape = s->modes[want].shape;
+            s->solve_fn = s->modes[want].fn;
+            s->grid = s->modes[want].grid;
+            s->draining = false;
+        } else if (s->mode == 0 && s->waiting.size() > (size_t)kQueueForBatchMode) {
+            s->draining = true;
+        }
+        while (!s->draining && !s->waiting.empty() && (int)admit.size() < s->max_admit && !s->free_slots.empty()) {
             Request* r = s->waiting.front();
             const size_t need = r->resident_bytes + r->transient_bytes;
             if (need > s->opt.hbm_budget_bytes) {  // can never fit
@@ -228,6 +261,7 @@ void tick(hd_server* s) {
                 continue;
             }
             if (s->stats.bytes_in_use + need > s->opt.hbm_budget_bytes) break;
+            r->nbricks = (unsigned long long)hdk::bricks_max(r->W, r->H, r->D, s->shape.bxw, s->shape.by, s->shape.bz);
             unsigned long long b0 = 0;
             if (!s->bricks.alloc(2 * r->nbricks, &b0)) break;
             s->waiting.pop_front();
@@ -558,6 +592,24 @@ void worker_main(hd_server* s) {
     }
 }
 
+// Polls `ready` (server lock held by `lk`, released between polls) for up
+// to kWaitSpinUs, or timeout_ms if that is shorter; true once it holds.  A
+// result that lands within the window is picked up without the
+// condition variable's wake-up latency.
+template <class F>
+bool spin_wait(hd_server* s, std::unique_lock<std::mutex>& lk, F ready, int64_t timeout_ms) {
+    const auto lim = std::chrono::microseconds(
+        timeout_ms >= 0 ? std::min<int64_t>(kWaitSpinUs, timeout_ms * 1000) : kWaitSpinUs);
+    const auto t0 = std::chrono::steady_clock::now();
+    while (!ready()) {
+        if (std::chrono::steady_clock::now() - t0 >= lim) return false;
+        lk.unlock();
+        lk.lock();
+    }
+    (void)s;
+    return true;
+}
+
 }  // namespace
 
 extern "C" {
@@ -598,21 +650,31 @@ hd_status hd_server_create(hd_context* ctx, const hd_server_options* opt, hd_ser
             return HD_ERR_CUDA;
         }
         PairIn typical{nullptr, nullptr, 256, 256, 160, nullptr, nullptr};
-        s->shape = pick_shape(ctx, s->se, &typical, 16);  // a batch-like mix of pairs
-        const int cps = s->shape.ctas_per_sm;
-        s->solve_fn = solve_fn_of(s->se, s->shape);
-        if (!s->solve_fn) {
-            delete s;
-            return HD_ERR_BAD_ARG;
+        unsigned long long brick_bytes = ~0ull;
+        for (int m = 0; m < 2; ++m) {
+            Shape sh = pick_shape(ctx, s->se, &typical, m == 0 ? 1 : 16);  // one pair / a batch-like mix
+            const void* fn = solve_fn_of(s->se, sh);
+            if (!fn) {
+                delete s;
+                return HD_ERR_BAD_ARG;
+            }
+            const int occ = occupancy_of(ctx, fn, sh.threads, sh.smem);
+            if (occ <= 0) {
+                delete s;
+                return HD_ERR_CUDA;
+            }
+            const int cps = sh.ctas_per_sm;
+            s->modes[m].shape = sh;
+            s->modes[m].fn = fn;
+            s->modes[m].grid = ctx->sm_count * (cps > 0 ? std::min(cps, occ) : occ);
+            brick_bytes = std::min<unsigned long long>(brick_bytes, 4ULL * sh.bxw * sh.by * sh.bz);
         }
-        const int occ = occupancy_of(ctx, s->solve_fn, s->shape.threads, s->shape.smem);
-        if (occ <= 0) {
-            delete s;
-            return HD_ERR_CUDA;
-        }
-        s->grid = ctx->sm_count * (cps > 0 ? std::min(cps, occ) : occ);
-        // brick ids: one per 3 x (brick bytes) of budget (each job brick spans 3 buffers), capped
-        const unsigned long long brick_bytes = 4ULL * s->shape.bxw * s->shape.by * s->shape.bz;
+        s->mode = 1;
+        s->shape = s->modes[1].shape;
+        s->solve_fn = s->modes[1].fn;
+        s->grid = s->modes[1].grid;
+        // brick ids: one per 3 x (brick bytes) of budget (each job brick
+        // spans 3 buffers) for the smaller brick of the two shapes, capped
         s->brick_cap = std::min<unsigned long long>(s->opt.hbm_budget_bytes / (3 * brick_bytes) + 4096, 1ULL << 26);
         s->bricks = RangeAlloc(s->brick_cap);
         cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
@@ -692,7 +754,7 @@ hd_status hd_server_submit(hd_server* s, const hd_pair_desc* pair, uint64_t* tic
     s->waiting.push_back(r.get());
     s->reqs[r->ticket] = std::move(r);
     s->stats.submitted += 1;
-    if (s->in_tick && !s->yield_posted) {
+    if (s->in_tick && !s->yield_posted && !s->draining) {
         // a tick is running: advance the yield word so that its launch ends
         // at the next grid barrier and the next tick admits this request.
         // The copy may read a later (larger) generation than the one written
@@ -727,6 +789,7 @@ hd_status hd_server_wait(hd_server* s, uint64_t ticket, int64_t timeout_ms, hd_r
     if (it == s->reqs.end()) return HD_ERR_BAD_ARG;
     Request* r = it->second.get();
     auto ready = [&] { return r->state == kDone; };
+    spin_wait(s, lk, ready, timeout_ms);
     if (timeout_ms < 0) {
         s->done_cv.wait(lk, ready);
     } else if (!s->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
@@ -745,6 +808,7 @@ hd_status hd_server_wait_any(hd_server* s, int64_t timeout_ms, uint64_t* ticket,
         while (!s->done_order.empty() && !s->reqs.count(s->done_order.front())) s->done_order.pop_front();
         if (!s->done_order.empty()) break;
         auto ready = [&] { return !s->done_order.empty(); };
+        if (spin_wait(s, lk, ready, timeout_ms)) continue;
         if (timeout_ms < 0) {
             s->done_cv.wait(lk, ready);
         } else if (!s->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
