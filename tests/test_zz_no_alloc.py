@@ -82,3 +82,27 @@ def test_noalloc_edge_cases_and_limit(ctx):
     code = L.hd_compute_u8_device_noalloc(z.data_ptr(), z.data_ptr(), 1024, 1024, 1024, N.HD_SE6, None,
                                           out.data_ptr())
     assert code == N.HD_ERR_BAD_ARG
+
+
+def test_noalloc_headline_pairs_against_oracle_fixtures():
+    """The 512x512x256 headline pairs (they fit the fixed array) straight
+    against the oracle's stored results for them (tests/golden/configs.json,
+    exact distance transforms and the restatement of the reference loop):
+    every field but the barrier-loop count, twice in a row."""
+    import json
+    import os
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, os.path.join(here, "golden"))
+    from make_config_golden import make_masks
+    fix = json.load(open(os.path.join(here, "golden", "configs.json")))["configs"]["c2"]
+    for _ in range(2):
+        for name in sorted(fix):
+            o = fix[name]["se6"]
+            a, b = make_masks(tuple(o["key"]), "cuda")
+            assert int(a.sum()) == o["n_a"] and int(b.sum()) == o["n_b"]
+            code, got = noalloc(a, b, N.HD_SE6)
+            assert code == N.HD_OK
+            for f in FIELDS:
+                if f != "iterations":
+                    assert got[f] == o[f], (name, f, got[f], o[f])
