@@ -159,3 +159,25 @@ def test_arrival_joins_a_running_tick(hd, ctx):
         got = dict([srv.wait_any(60000), srv.wait_any(60000)])
     assert most == 2, "the second pair was not admitted while the first one ran"
     assert same(got[ts], want_small) and same(got[tb], want_big)
+
+
+def test_lone_request_then_burst_switches_kernel_shape(hd, ctx):
+    """A lone request starts a busy period in the single-pair kernel shape; a
+    burst submitted behind it makes the server drain and continue in the
+    batch shape.  Every result equals the plain path, and a second lone
+    request after the burst runs in the single-pair shape again."""
+    lone = _pairs(1, 37, lo=96, hi=128, edge=0.0)[0]
+    burst = _pairs(30, 41, lo=32, hi=96, edge=0.1)
+    want_lone = ctx.compute(*lone, "se6")
+    want = [ctx.compute(a, b, "se6") for a, b in burst]
+    with hd.Server(ctx) as srv:
+        t0 = srv.submit(*lone)
+        time.sleep(0.0005)
+        ts = [srv.submit(a, b) for a, b in burst]
+        res = [srv.wait(t, 60000) for t in ts]
+        r0 = srv.wait(t0, 60000)
+        time.sleep(0.002)
+        r1 = srv.wait(srv.submit(*lone), 60000)
+    assert same(r0, want_lone) and same(r1, want_lone)
+    for i, (r, w) in enumerate(zip(res, want)):
+        assert same(r, w), i
