@@ -393,6 +393,7 @@ def bench_ours(args):
         # every rank: the 256-pair ragged batch split over the ranks
         out["sharded_batch"] = bench_sharded_batch(ctx, args, ws, rank, dist)
     if rank == 0 and ws == 1 and not args.no_extras:
+        out["drop_in_default_element"] = bench_se18(ctx, pairs, seed)
         out["batched"] = bench_batched(ctx, args)
         out["worst_case"] = bench_worst_case(ctx, dev)
         out["serving"] = bench_serving(ctx, args)
@@ -515,6 +516,31 @@ def bench_batched(ctx, args):
                   "brick_words_rows_planes": [bt["brick_x_words"], bt["brick_rows"], bt["brick_z"]],
                   "grid_ctas": bt["grid_ctas"]},
     }
+
+
+def bench_se18(ctx, pairs, seed):
+    """The headline pairs under the 18-neighbour element, the C++ drop-in's
+    default (CHEBYSHEV 1): it runs on the whole volume (no bounding-box
+    crop), through the blocking device entry; each result checked against
+    the oracle's."""
+    import torch
+    stream = torch.cuda.current_stream()
+    ts, hds, checked = [], [], 0
+    for i, (x, y) in enumerate(pairs):
+        r = ctx.compute(x, y, "se18")
+        checked += _check_fixture(r, "c2", f"pair{i}_seed{seed + i}", "se18", f"headline pair {i}, 18-neighbour element")
+        hds.append(r["hd"])
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.compute(x, y, "se18")
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+    t = statistics.median(ts)
+    return {"workload": "the two headline pairs, 18-neighbour element (forBench CHEBYSHEV 1), whole volume",
+            "hd": hds, "ms_per_pair": round(t, 4), "pairs_per_s": round(1000.0 / t, 1),
+            "path": "hd_compute_u8_device (blocking, result on the host)", "pairs_checked_against_oracle": int(checked)}
 
 
 def bench_sharded_batch(ctx, args, ws, rank, dist):

@@ -58,7 +58,7 @@ struct Request {
     int kmax = 0;
     int wxf = 0;
     long long dom_words = 0;
-    size_t off_hist = 0, off_info = 0;
+    size_t off_hist = 0, off_info = 0, off_packed = 0;
 };
 
 // First-fit allocator over [0, cap) (brick ids).
@@ -183,8 +183,9 @@ hd_status cuda_err(hd_server* s, cudaError_t e, const char* where) {
 // transient part only through packing and set-up).  Resident: three
 // domain-sized buffers per job (both ping-pong buffers, and the
 // uncovered-target array of the one-step kernel or a crop of one mask for
-// the blocked kernel), histograms, counts.  Transient: the packed masks and
-// the staged host masks.
+// the blocked kernel), histograms, counts, and the packed masks, which the
+// blocked kernel reads in place as the single-pair path does (no crop copy
+// in set-up).  Transient: the staged host masks.
 void plan_request(hd_server* s, Request* r) {
     r->wxf = (r->W + 31) / 32;
     const long long pitch = (r->wxf + 3) / 4 * 4;
@@ -193,10 +194,11 @@ void plan_request(hd_server* s, Request* r) {
     const size_t job_bytes = align_up(4ULL * r->dom_words);
     r->off_hist = 6 * job_bytes;
     r->off_info = align_up(r->off_hist + 2ULL * (r->kmax + 1) * sizeof(uint64_t));
-    r->resident_bytes = align_up(r->off_info + sizeof(PairInfo));
+    r->off_packed = align_up(r->off_info + sizeof(PairInfo));
     const size_t nb = (size_t)r->W * r->H * r->D;
     const size_t packed = align_up(4ULL * hdk::packed_pitch(r->W) * r->H * r->D);
-    r->transient_bytes = 2 * packed + (r->dev_a ? 0 : 2 * align_up(nb));
+    r->resident_bytes = r->off_packed + 2 * packed;
+    r->transient_bytes = r->dev_a ? 0 : 2 * align_up(nb);
 }
 
 // Marks a request done (server lock held) and lists it for wait_any.
@@ -290,11 +292,12 @@ void tick(hd_server* s) {
     std::vector<PairDesc> descs;
     std::vector<Request*> admitted;
     long long ptiles = 0, stiles = 0;
-    // the packed masks are freed after set-up: the blocked kernel reads crops
-    const int setup_mode = s->shape.kernel == 1 ? hdk::kSetupOneStep : hdk::kSetupBlockedCrop;
-    // the admitted pairs' transient buffers (packed masks, staged host masks)
-    // in one block for the tick, freed after the set-up; a block per pair
-    // for what lives until the pair completes
+    // the blocked kernel reads the packed masks in place unless that adds a
+    // brick column (then crops), like the single-pair path
+    const int setup_mode = s->shape.kernel == 1 ? hdk::kSetupOneStep : hdk::kSetupBlocked;
+    // the admitted pairs' transient buffers (staged host masks) in one block
+    // for the tick, freed after the set-up; a block per pair for what lives
+    // until the pair completes
     size_t transient_total = 0;
     for (Request* r : admit) transient_total += align_up(r->transient_bytes);
     void* tblock = nullptr;
@@ -309,8 +312,9 @@ void tick(hd_server* s) {
     for (size_t i = 0; i < admit.size(); ++i) {
         Request* r = admit[i];
         void* res = nullptr;
-        if (tblock) e = cudaMallocFromPoolAsync(&res, r->resident_bytes, s->pool, st);
-        if (!tblock || e != cudaSuccess) {
+        const bool t_ok = tblock != nullptr || transient_total == 0;
+        if (t_ok) e = cudaMallocFromPoolAsync(&res, r->resident_bytes, s->pool, st);
+        if (!t_ok || e != cudaSuccess) {
             cudaGetLastError();
             e = cudaSuccess;
             std::lock_guard<std::mutex> lk(s->mu);
@@ -323,7 +327,7 @@ void tick(hd_server* s) {
         }
         r->resident = res;
         char* rb = (char*)res;
-        char* tb = (char*)tblock + toff;
+        char* tb = tblock ? (char*)tblock + toff : nullptr;
         toff += align_up(r->transient_bytes);
         const size_t nb = (size_t)r->W * r->H * r->D;
         const size_t packed = align_up(4ULL * hdk::packed_pitch(r->W) * r->H * r->D);
@@ -332,15 +336,15 @@ void tick(hd_server* s) {
             d.a = r->dev_a;
             d.b = r->dev_b;
         } else {
-            uint8_t* ia = (uint8_t*)(tb + 2 * packed);
+            uint8_t* ia = (uint8_t*)tb;
             uint8_t* ib = ia + align_up(nb);
             cudaMemcpyAsync(ia, r->host_a.data(), nb, cudaMemcpyHostToDevice, st);
             cudaMemcpyAsync(ib, r->host_b.data(), nb, cudaMemcpyHostToDevice, st);
             d.a = ia;
             d.b = ib;
         }
-        d.pa = (uint32_t*)tb;
-        d.pb = (uint32_t*)(tb + packed);
+        d.pa = (uint32_t*)(rb + r->off_packed);
+        d.pb = (uint32_t*)(rb + r->off_packed + packed);
         const size_t job_bytes = align_up(4ULL * r->dom_words);
         for (int j = 0; j < 2; ++j) {
             for (int b = 0; b < 3; ++b) d.jb[j][b] = (uint32_t*)(rb + (3 * j + b) * job_bytes);
