@@ -601,7 +601,7 @@ void worker_main(hd_server* s) {
 // result that lands within the window is picked up without the
 // condition variable's wake-up latency.
 template <class F>
-bool spin_wait(hd_server* s, std::unique_lock<std::mutex>& lk, F ready, int64_t timeout_ms) {
+bool spin_wait(std::unique_lock<std::mutex>& lk, F ready, int64_t timeout_ms) {
     const auto lim = std::chrono::microseconds(
         timeout_ms >= 0 ? std::min<int64_t>(kWaitSpinUs, timeout_ms * 1000) : kWaitSpinUs);
     const auto t0 = std::chrono::steady_clock::now();
@@ -610,7 +610,6 @@ bool spin_wait(hd_server* s, std::unique_lock<std::mutex>& lk, F ready, int64_t 
         lk.unlock();
         lk.lock();
     }
-    (void)s;
     return true;
 }
 
@@ -793,7 +792,7 @@ hd_status hd_server_wait(hd_server* s, uint64_t ticket, int64_t timeout_ms, hd_r
     if (it == s->reqs.end()) return HD_ERR_BAD_ARG;
     Request* r = it->second.get();
     auto ready = [&] { return r->state == kDone; };
-    spin_wait(s, lk, ready, timeout_ms);
+    spin_wait(lk, ready, timeout_ms);
     if (timeout_ms < 0) {
         s->done_cv.wait(lk, ready);
     } else if (!s->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
@@ -812,7 +811,7 @@ hd_status hd_server_wait_any(hd_server* s, int64_t timeout_ms, uint64_t* ticket,
         while (!s->done_order.empty() && !s->reqs.count(s->done_order.front())) s->done_order.pop_front();
         if (!s->done_order.empty()) break;
         auto ready = [&] { return !s->done_order.empty(); };
-        if (spin_wait(s, lk, ready, timeout_ms)) continue;
+        if (spin_wait(lk, ready, timeout_ms)) continue;
         if (timeout_ms < 0) {
             s->done_cv.wait(lk, ready);
         } else if (!s->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
