@@ -636,7 +636,6 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     // ---- pack, set-up -----------------------------------------------------
     // one CTA per tile up to 8 per SM, then striding
     const int grid_pack = (int)std::min<long long>(std::max(prep_sms * 8, 1), pack_tiles);
-    const int grid_setup = (int)std::min<long long>(std::max(prep_sms * 8, 1), setup_tiles);
     const PairDesc* ddesc = (const PairDesc*)(dbase + off_descs);
     const bool timing = ctx->opt.record_timings != 0 && ctx->ev[0] != nullptr && !async;
     if (timing) cudaEventRecord(ctx->ev[0], s);
@@ -654,7 +653,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
                                  (unsigned long long*)(dbase + off_q[2])};
     if (timing) cudaEventRecord(ctx->ev[1], s);
     if (stime) cudaEventRecord(ctx->split.ev[1], sq);
-    e = hdk::launch_setup(ddesc, n, setup_tiles, grid_setup, djobs, dstates, dq[g0 % 3], dctl, g0, bxw, by, bz,
+    e = hdk::launch_setup(ddesc, n, setup_tiles, split ? prep_sms : 0, djobs, dstates, dq[g0 % 3], dctl, g0, bxw, by, bz,
                           setup_mode, sq);
     if (e == cudaSuccess && split) {
         // the dilation follows the set-up; the caller's stream follows the

@@ -13,11 +13,11 @@ namespace hdk {
 // setup_tiles_of) with `grid` CTAs.  Brick geometry: bxw words x by rows x
 // bz planes (both kernel families).
 // label: 0 = every nonzero byte is foreground, 1..255 = bytes equal to label.
-// sms: SMs the stream's kernels run on (0: the device's); the grid is one
-// resident wave of them.
+// sms (packing and set-up): SMs the stream's kernels run on (0: the
+// device's); the grid is one resident wave of them.
 cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, int grid, int label, int sms,
                         cudaStream_t s);
-cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int grid, Job* jobs,
+cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int sms, Job* jobs,
                          JobState* states, unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
                          int mode, cudaStream_t s);
 // Start values of descs[i].info (counts 0, empty bounding box), i < npairs;

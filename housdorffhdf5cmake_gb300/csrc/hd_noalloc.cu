@@ -176,7 +176,7 @@ extern "C" hd_status hd_compute_u8_device_noalloc(const uint8_t* d_a, const uint
     unsigned long long* q[3] = {(unsigned long long*)(base + L.queue[0]), (unsigned long long*)(base + L.queue[1]),
                                 (unsigned long long*)(base + L.queue[2])};
     if (e == cudaSuccess)
-        e = hdk::launch_setup(desc, 1, stiles, (int)std::min<long long>(cap_ctas, stiles), jobs, states, q[g0 % 3], ctl,
+        e = hdk::launch_setup(desc, 1, stiles, 0, jobs, states, q[g0 % 3], ctl,
                               g0, kBxw, 32 / kBxw, kBz, hdk::kSetupOneStep, s);
     if (e == cudaSuccess) {
         hdk::SolveParams sp{};

@@ -396,9 +396,9 @@ __device__ __forceinline__ bool blocked_in_place(const PairDesc& P, const PairIn
     return (w1 - I.bb[0] + 3) / 4 == (w1 - (I.bb[0] & ~3) + 3) / 4;
 }
 
-__device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_pair, Job* jobs, JobState* states,
-                                           unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
-                                           int mode, unsigned* s_base);
+__device__ __forceinline__ long long setup_tile(const PairDesc& P, long long tile_in_pair, Job* jobs,
+                                                JobState* states, unsigned long long* queue0, Ctl* ctl, int g0,
+                                                int bxw, int by, int bz, int mode, unsigned* s_base);
 
 // 1D grid, block 256: CTAs stride over the tiles of all pairs
 // (setup_tiles_of per pair); tile 0 of a pair also writes its job
@@ -418,19 +418,33 @@ __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__
                                                     Ctl* ctl, int g0, int bxw, int by, int bz, int mode) {
     __shared__ unsigned s_base;
     int pi = -1;
+    const long long G = gridDim.x;
     // CTAs stride over the tiles: a pair's domain fills only the first of
     // its tiles, so contiguous runs would leave some CTAs without work
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (long long tile = blockIdx.x; tile < ntiles; tile += G) {
         int np = pi < 0 ? pair_of_tile(descs, npairs, tile, true) : pi;
         while (np + 1 < npairs && descs[np + 1].stile0 <= tile) ++np;  // tiles only increase
         pi = np;
-        setup_tile(descs[pi], tile - descs[pi].stile0, jobs, states, queue0, ctl, g0, bxw, by, bz, mode, &s_base);
+        const long long t0 = descs[pi].stile0;
+        const long long need = setup_tile(descs[pi], tile - t0, jobs, states, queue0, ctl, g0, bxw, by, bz, mode,
+                                          &s_base);
+        // The pair's tiles from `need` on have nothing to do (the host sizes
+        // the tiles for the largest domain and for copies that reading the
+        // packed masks in place makes unnecessary): continue at this CTA's
+        // first tile of the next pair.  CTA-uniform.
+        if (tile - t0 + G >= need) {
+            const long long next0 = pi + 1 < npairs ? descs[pi + 1].stile0 : ntiles;
+            const long long first = next0 + ((((long long)blockIdx.x - next0) % G) + G) % G;  // >= tile + G
+            tile = first - G;
+        }
     }
 }
 
-__device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_pair, Job* jobs, JobState* states,
-                                           unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
-                                           int mode, unsigned* s_base) {
+// Returns the number of tiles of the pair that have work (descriptors,
+// copies or queue entries): later tiles return at once.
+__device__ __forceinline__ long long setup_tile(const PairDesc& P, long long tile_in_pair, Job* jobs,
+                                                JobState* states, unsigned long long* queue0, Ctl* ctl, int g0,
+                                                int bxw, int by, int bz, int mode, unsigned* s_base) {
     const PairInfo I = *P.info;
     const bool empty_a = I.n_a == 0, empty_b = I.n_b == 0;
     const unsigned long long rem[2] = {I.n_b - I.n_ab, I.n_a - I.n_ab};
@@ -457,7 +471,7 @@ __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_
                 J.epoch = P.epoch;
             }
         }
-        return;
+        return 1;
     }
     const bool one_step = mode == kSetupOneStep;
     const bool in_place = mode == kSetupBlockedInPlace || (mode == kSetupBlocked && blocked_in_place(P, I));
@@ -509,7 +523,8 @@ __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_
     }
     // Crop copy.  Job 0 dilates A and must cover B; job 1 dilates B and covers A.
     const bool act0 = rem[0] > 0, act1 = rem[1] > 0;
-    const long long words = (one_step || !in_place) ? min((long long)m.pitch * m.h * m.d, w_hi) : 0;
+    const long long words_all = (one_step || !in_place) ? (long long)m.pitch * m.h * m.d : 0;
+    const long long words = min(words_all, w_hi);
     const int vpitch = packed_pitch(P.W);
     for (long long t = w_lo + tid0; t < words; t += nthr) {
         // domain word index < 2^31: 32-bit divisions
@@ -547,7 +562,8 @@ __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_
     const long long b_per = mode == kSetupBlockedInPlace ? kSetupBricks
                                                           : (b_even > 256 ? b_even : 256);  // < 2^31 bricks, tiles
     const long long b_lo = tile_in_pair * b_per, b_hi = min(nbricks, b_lo + b_per);
-    if (b_lo >= b_hi) return;  // CTA-uniform
+    const long long need = max(max((words_all + kTileWords - 1) / kTileWords, (nbricks + b_per - 1) / b_per), 1ll);
+    if (b_lo >= b_hi) return need;  // CTA-uniform
     for (int j = 0; j < 2; ++j) {
         if (!(j == 0 ? act0 : act1)) continue;
         if (tid0 == 0) *s_base = atomicAdd(&ctl->qcount[g0 % 3], (unsigned)(b_hi - b_lo));
@@ -557,6 +573,7 @@ __device__ __forceinline__ void setup_tile(const PairDesc& P, long long tile_in_
             queue0[base + (unsigned)(t - b_lo)] = make_entry(P.epoch, (uint32_t)(P.job0 + j), (uint32_t)t);
         __syncthreads();  // s_base is written again next
     }
+    return need;
 }
 
 // Start values of each pair's counts and bounding box (one thread per pair).
@@ -636,12 +653,35 @@ cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, i
     return cudaGetLastError();
 }
 
-cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int grid, Job* jobs,
+cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int sms, Job* jobs,
                          JobState* states, unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
                          int mode, cudaStream_t s) {
-    if (grid > ntiles) grid = (int)ntiles;
+    // one wave of resident CTAs (per device, from the occupancy calculator):
+    // CTAs whose tiles have nothing to do leave at once, later waves would
+    // only add their scheduling
+    static int per_sm_of[64] = {0};
+    static int sms_of[64] = {0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    int per_sm = 8, nsm = sms > 0 ? sms : 1;
+    if (dev < 64) {
+        if (per_sm_of[dev] == 0) {
+            int occ = 0, sms_dev = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, reinterpret_cast<const void*>(&setup_kernel), 256,
+                                                              0);
+            if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms_dev, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return e;
+            per_sm_of[dev] = std::max(1, occ);
+            sms_of[dev] = std::max(1, sms_dev);
+        }
+        per_sm = per_sm_of[dev];
+        if (sms <= 0) nsm = sms_of[dev];
+    }
+    long long grid = std::min<long long>((long long)per_sm * nsm, ntiles);
     if (grid < 1) grid = 1;
-    setup_kernel<<<grid, 256, 0, s>>>(d_descs, npairs, ntiles, jobs, states, queue0, ctl, g0, bxw, by, bz, mode);
+    setup_kernel<<<(unsigned)grid, 256, 0, s>>>(d_descs, npairs, ntiles, jobs, states, queue0, ctl, g0, bxw, by, bz,
+                                                mode);
     return cudaGetLastError();
 }
 

@@ -379,7 +379,7 @@ void tick(hd_server* s) {
             e = hdk::launch_pack(s->d_descs, (int)admitted.size(), ptiles, (int)std::min<long long>(cap_ctas, ptiles),
                                  s->ctx->opt.label, 0, st);
         if (e == cudaSuccess)
-            e = hdk::launch_setup(s->d_descs, (int)admitted.size(), stiles, (int)std::min<long long>(cap_ctas, stiles),
+            e = hdk::launch_setup(s->d_descs, (int)admitted.size(), stiles, 0,
                                   s->d_jobs, s->d_states,
                                   s->d_queue[s->g_next % 3], s->d_ctl, s->g_next, s->shape.bxw, s->shape.by,
                                   s->shape.bz, setup_mode, st);
