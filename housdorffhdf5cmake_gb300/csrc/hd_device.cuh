@@ -75,20 +75,30 @@ constexpr long long kPackTileWords = 1024;
 // Temporally blocked dilation kernel (hd_solve_tb.cuh): each warp streams
 // the BZ + 2T planes of its brick through a ring of shared-memory slots
 // kTbPrefetch planes ahead of the one being computed; a plane stays until
-// its final step has been compared with it, T planes later.  Per warp: the
-// slots (32 rows x (16 B interior + 8 B halo words)) and the brick's
-// target rows (BZ planes x 32 rows x 16 B).  CTAs of kTbWarps warps per
-// SM: 3, and 4 for 1 or 2 steps per barrier (registers capped at 128 per
-// thread), whose work per barrier is large enough for more warps to hide
-// the latency of the planes' dependency chains.
+// its final step has been compared with it, T planes later.  A lane holds
+// tb_rows(T) consecutive rows of the brick (the warp 32 tb_rows(T) rows, 2T
+// of them halo): a row's neighbours in y come from the lane's own registers
+// but for the first and last row, which take one shuffle each.  Per warp:
+// the slots (32 tb_rows rows x (16 B interior + 8 B halo words)) and the
+// brick's target rows (BZ planes x 32 tb_rows rows x 16 B).  Resident CTAs
+// of kTbWarps warps per SM: tb_min_ctas (the registers of the levels' state
+// decide).
 constexpr int kTbWarps = 4;
 constexpr int kTbPrefetch = 2;
-__host__ __device__ constexpr int tb_min_ctas(int T) { return T <= 2 ? 4 : 3; }
+// One row per lane: two (half the shuffles per row, a 64-row block with 2T
+// halo rows) measured slower on every workload (218 registers at 4 steps,
+// 2 CTAs per SM: 512x512x256 0.129 against 0.113 ms, 512^3 5.7 against 3.8
+// ms, the ragged batch 2.35 against 1.54 ms).
+__host__ __device__ constexpr int tb_rows(int) { return 1; }
+__host__ __device__ constexpr int tb_min_ctas(int T) {
+    return tb_rows(T) == 1 ? (T <= 2 ? 4 : 3) : (T <= 2 ? 3 : 2);
+}
+__host__ __device__ constexpr int tb_brick_rows(int T) { return 32 * tb_rows(T) - 2 * T; }
 __host__ __device__ constexpr int tb_ring_slots(int T, int BZ) {
     return T + 1 + kTbPrefetch >= BZ + 2 * T ? BZ + 2 * T : T + 1 + kTbPrefetch;
 }
 __host__ __device__ constexpr int tb_warp_bytes(int T, int BZ) {
-    return tb_ring_slots(T, BZ) * 32 * 24 + BZ * 32 * 16;
+    return (tb_ring_slots(T, BZ) * 32 * 24 + BZ * 32 * 16) * tb_rows(T);
 }
 __host__ __device__ __forceinline__ long long pack_words(int W, int H, int D) {
     return (long long)((W + 31) / 32) * H * D;

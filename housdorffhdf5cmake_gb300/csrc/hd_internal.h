@@ -51,7 +51,7 @@ struct Shape {  // default: the autotuner's choice on the 512x512x256, 512^3 and
             // kTbWarps warps per CTA, each with a ring of streamed planes and
             // the brick's target rows in shared memory
             bxw = 4;
-            by = 32 - 2 * steps;
+            by = hdk::tb_brick_rows(steps);
             threads = hdk::kTbWarps * 32;
             smem = hdk::kTbWarps * hdk::tb_warp_bytes(steps, bz);
         } else {

@@ -64,17 +64,20 @@ __device__ __forceinline__ void cp_async_wait_upto(int n) {
 // Shared memory of one warp: ring slots of streamed planes (interior words
 // as 16-byte rows, then the two halo words of each row), then the brick's
 // target rows (18-neighbour element: target minus state, updated per level).
+// Row k of every lane is contiguous within a slot (lane-consecutive 16-byte
+// rows: conflict-free 128-bit accesses).
 template <int T, int BZ>
 struct TbSmem {
+    static constexpr int R = tb_rows(T);    // rows per lane
     static constexpr int NP = BZ + 2 * T;  // planes streamed per brick
-    static constexpr int R = tb_ring_slots(T, BZ);
+    static constexpr int RS = tb_ring_slots(T, BZ);
     static constexpr int PF = kTbPrefetch;  // planes in flight ahead of the one computed
-    static constexpr int kInBytes = R * 32 * 16;
-    static constexpr int kHaloBytes = R * 32 * 8;
+    static constexpr int kInBytes = RS * R * 32 * 16;
+    static constexpr int kHaloBytes = RS * R * 32 * 8;
     static constexpr int kUOff = kInBytes + kHaloBytes;
-    static constexpr int kWarpBytes = kUOff + BZ * 32 * 16;
+    static constexpr int kWarpBytes = kUOff + BZ * R * 32 * 16;
     static_assert(kWarpBytes == tb_warp_bytes(T, BZ), "shared layout");
-    static_assert(R >= T + 1 + PF || R == NP, "a plane must stay until its final step");
+    static_assert(RS >= T + 1 + PF || RS == NP, "a plane must stay until its final step");
 };
 
 // One queue item of the blocked kernel, decoded.
@@ -90,67 +93,73 @@ struct TbItem {
     bool live;
 };
 
-// Where this lane's row of a streamed plane comes from: domain plane z, row
+// Where this lane's rows of a streamed plane come from: domain plane z, row
 // y, words wx0 .. wx0 + 3 of the brick are at src + (z + zoff) * plane +
-// rowoff.  The level-0 state is the job's ping-pong buffer, except in the
-// job's first iteration, which reads the source (vol[0]); the target always
-// comes from vol[1].  Every row copy is one 16-byte copy: the domain layout
-// and the packed masks (rows padded to a multiple of 4 words, read in place
-// only when the domain starts on a multiple of 4 words) keep a brick's 4
-// words in its row, and those past the domain are row padding or outside
-// the bounding box of A u B (zero).
+// rowoff[k] for the lane's row k (brick row R lane + k).  The level-0 state
+// is the job's ping-pong buffer, except in the job's first iteration, which
+// reads the source (vol[0]); the target always comes from vol[1].  Every
+// row copy is one 16-byte copy: the domain layout and the packed masks (rows
+// padded to a multiple of 4 words, read in place only when the domain starts
+// on a multiple of 4 words) keep a brick's 4 words in its row, and those past
+// the domain are row padding or outside the bounding box of A u B (zero).
+template <int R>
 struct TbRow {
     const uint32_t* src;
-    int plane, rowoff, zoff, z0, Dd;
-    bool rowv, hl_ok, hr_ok;
+    int plane, zoff, z0, Dd;
+    int rowoff[R];
+    bool rowv[R], hl_ok[R], hr_ok[R];
 };
 
 template <int T, int BZ>
-__device__ __forceinline__ TbRow tb_row(const TbItem& it, bool target) {
+__device__ __forceinline__ TbRow<tb_rows(T)> tb_row(const TbItem& it, bool target) {
     constexpr int IW = 4;
-    constexpr int BYI = 32 - 2 * T;
+    constexpr int R = tb_rows(T);
+    constexpr int BYI = tb_brick_rows(T);
     const int lane = threadIdx.x & 31;
     const Job* Jp = it.Jp;
-    TbRow w;
+    TbRow<R> w;
     const int Wx = Jp->wx, Hd = Jp->h;
     const int wx0 = it.bx * IW;
-    const int y = it.by * BYI - T + lane;
-    w.rowv = y >= 0 && y < Hd;
-    const int yc = w.rowv ? y : 0;
-    if (target || it.iter == 0) {
-        w.src = Jp->vol[target ? 1 : 0];
-        w.plane = Jp->vpitch * Jp->vh;
-        w.rowoff = (yc + Jp->vy0) * Jp->vpitch + Jp->vx0 + wx0;
-        w.zoff = Jp->vz0;
-    } else {
-        w.src = Jp->buf[it.iter & 1];
-        w.plane = Jp->pitch * Hd;
-        w.rowoff = yc * Jp->pitch + wx0;
-        w.zoff = 0;
+    const bool first = target || it.iter == 0;
+    const int pitch = first ? Jp->vpitch : Jp->pitch;
+    const int rbase = first ? Jp->vy0 : 0;
+    const int xbase = (first ? Jp->vx0 : 0) + wx0;
+    w.src = first ? Jp->vol[target ? 1 : 0] : Jp->buf[it.iter & 1];
+    w.plane = first ? Jp->vpitch * Jp->vh : Jp->pitch * Hd;
+    w.zoff = first ? Jp->vz0 : 0;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int y = it.by * BYI - T + lane * R + k;
+        w.rowv[k] = y >= 0 && y < Hd;
+        w.rowoff[k] = ((w.rowv[k] ? y : 0) + rbase) * pitch + xbase;
+        w.hl_ok[k] = w.rowv[k] && wx0 > 0;
+        w.hr_ok[k] = w.rowv[k] && wx0 + IW < Wx;
     }
     w.z0 = it.bz * BZ;
     w.Dd = Jp->d;
-    w.hl_ok = w.rowv && wx0 > 0;
-    w.hr_ok = w.rowv && wx0 + IW < Wx;
     return w;
 }
 
 // Copies streamed plane r of the brick into its ring slot (one group).
 template <int T, int BZ>
-__device__ __forceinline__ void tb_copy_plane(const TbRow& w, int r, unsigned char* wsm) {
+__device__ __forceinline__ void tb_copy_plane(const TbRow<tb_rows(T)>& w, int r, unsigned char* wsm) {
     using SM = TbSmem<T, BZ>;
     constexpr int IW = 4;
     const int lane = threadIdx.x & 31;
     const int z = w.z0 - T + r;
-    const bool ok = w.rowv && z >= 0 && z < w.Dd;
-    const uint32_t* gp = w.src + (ok ? (z + w.zoff) * w.plane + w.rowoff : 0);
-    const int slot = r % SM::R;
+    const bool zok = z >= 0 && z < w.Dd;
+    const int slot = r % SM::RS;
     const uint32_t base = (uint32_t)__cvta_generic_to_shared(wsm);
-    const uint32_t s_in = base + (uint32_t)((slot * 32 + lane) * 16);
-    const uint32_t s_h = base + SM::kInBytes + (uint32_t)((slot * 32 + lane) * 8);
-    cp_async16(s_in, gp, ok ? 16u : 0u);
-    cp_async4(s_h, (ok && w.hl_ok) ? gp - 1 : gp, (ok && w.hl_ok) ? 4u : 0u);
-    cp_async4(s_h + 4, (ok && w.hr_ok) ? gp + IW : gp, (ok && w.hr_ok) ? 4u : 0u);
+#pragma unroll
+    for (int k = 0; k < SM::R; ++k) {
+        const bool ok = w.rowv[k] && zok;
+        const uint32_t* gp = w.src + (ok ? (z + w.zoff) * w.plane + w.rowoff[k] : 0);
+        const uint32_t s_in = base + (uint32_t)(((slot * SM::R + k) * 32 + lane) * 16);
+        const uint32_t s_h = base + SM::kInBytes + (uint32_t)(((slot * SM::R + k) * 32 + lane) * 8);
+        cp_async16(s_in, gp, ok ? 16u : 0u);
+        cp_async4(s_h, (ok && w.hl_ok[k]) ? gp - 1 : gp, (ok && w.hl_ok[k]) ? 4u : 0u);
+        cp_async4(s_h + 4, (ok && w.hr_ok[k]) ? gp + IW : gp, (ok && w.hr_ok[k]) ? 4u : 0u);
+    }
     cp_async_commit();
 }
 
@@ -207,19 +216,23 @@ __device__ __forceinline__ void tb_issue(const SolveParams& p, unsigned long lon
     const int lane = threadIdx.x & 31;
     if (!tb_decode<T>(p, e, g, it)) return;
     {
-        const TbRow t = tb_row<T, BZ>(it, true);
-        const bool inter = t.rowv && lane >= T && lane < 32 - T;
+        const TbRow<SM::R> t = tb_row<T, BZ>(it, true);
         const uint32_t s_u = (uint32_t)__cvta_generic_to_shared(wsm) + SM::kUOff;
 #pragma unroll
-        for (int i = 0; i < BZ; ++i) {
-            const int z = t.z0 + i;
-            const bool ok = inter && z < t.Dd;
-            cp_async16(s_u + (uint32_t)((i * 32 + lane) * 16), t.src + (ok ? (z + t.zoff) * t.plane + t.rowoff : 0),
-                       ok ? 16u : 0u);
+        for (int k = 0; k < SM::R; ++k) {
+            const int yr = lane * SM::R + k;  // row of the streamed block
+            const bool inter = t.rowv[k] && yr >= T && yr < 32 * SM::R - T;
+#pragma unroll
+            for (int i = 0; i < BZ; ++i) {
+                const int z = t.z0 + i;
+                const bool ok = inter && z < t.Dd;
+                cp_async16(s_u + (uint32_t)(((i * SM::R + k) * 32 + lane) * 16),
+                           t.src + (ok ? (z + t.zoff) * t.plane + t.rowoff[k] : 0), ok ? 16u : 0u);
+            }
         }
         cp_async_commit();
     }
-    const TbRow w = tb_row<T, BZ>(it, false);
+    const TbRow<SM::R> w = tb_row<T, BZ>(it, false);
 #pragma unroll
     for (int r = 0; r < SM::PF && r < SM::NP; ++r) tb_copy_plane<T, BZ>(w, r, wsm);
 }
@@ -246,7 +259,9 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
     static_assert(T >= 1 && T <= kTbMaxSteps && kTbMaxSteps < 16, "steps per barrier out of range");
     constexpr int IW = 4;
     constexpr int NW = IW + 1;  // [combined halo word, 4 interior words]
-    constexpr int BYI = 32 - 2 * T;
+    constexpr int R = tb_rows(T);
+    constexpr int ROWS = 32 * R;  // rows of the streamed block
+    constexpr int BYI = tb_brick_rows(T);
     using SM = TbSmem<T, BZ>;
     constexpr int NP = SM::NP;
     const int lane = threadIdx.x & 31;
@@ -256,49 +271,60 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
         cp_async_wait<0>();
         return;
     }
-    const TbRow w = tb_row<T, BZ>(it, false);
+    const TbRow<R> w = tb_row<T, BZ>(it, false);
     const int Wx = Jp->wx;
     const int wx0 = it.bx * IW;
-    const bool inter = w.rowv && lane >= T && lane < 32 - T;
+    bool inter[R];  // the lane's rows that belong to the brick (not halo, inside the domain)
+#pragma unroll
+    for (int k = 0; k < R; ++k) inter[k] = w.rowv[k] && lane * R + k >= T && lane * R + k < ROWS - T;
     uint32_t* __restrict__ dst = Jp->buf[(it.iter + 1) & 1];
     uint32_t* __restrict__ dst2 = it.iter == 0 ? Jp->buf[0] : nullptr;
     const int bplane = Jp->pitch * Jp->h;
-    const int browoff = (w.rowv ? it.by * BYI - T + lane : 0) * Jp->pitch + wx0;
-    uint32_t wm[NW];  // valid bits of each word of this lane's row
+    const int brow0 = it.by * BYI - T + lane * R;  // block row of the lane's row 0
+    uint32_t wmx[NW];  // valid bits of each word of a row (x only)
     {
         uint32_t w6[IW + 2];
 #pragma unroll
         for (int j = 0; j < IW + 2; ++j) {
             const int x = wx0 - 1 + j;
-            w6[j] = (w.rowv && x >= 0 && x < Wx) ? (x == Wx - 1 ? Jp->tailmask : kFull) : 0u;
+            w6[j] = (x >= 0 && x < Wx) ? (x == Wx - 1 ? Jp->tailmask : kFull) : 0u;
         }
-        wm[0] = (w6[0] & 0xffff0000u) | (w6[IW + 1] & 0x0000ffffu);
+        wmx[0] = (w6[0] & 0xffff0000u) | (w6[IW + 1] & 0x0000ffffu);
 #pragma unroll
-        for (int j = 1; j <= IW; ++j) wm[j] = w6[j];
+        for (int j = 1; j <= IW; ++j) wmx[j] = w6[j];
     }
 
     auto plane_ok = [&](int r) {  // streamed plane index r -> inside the domain
         const int z = w.z0 - T + r;
         return z >= 0 && z < w.Dd;
     };
-    auto in_row = [&](int r) -> uint4 {
-        return *reinterpret_cast<const uint4*>(wsm + ((r % SM::R) * 32 + lane) * 16);
+    auto in_row = [&](int r, int k) -> uint4 {
+        return *reinterpret_cast<const uint4*>(wsm + (((r % SM::RS) * R + k) * 32 + lane) * 16);
     };
-    auto halo_row = [&](int r) -> uint2 {
-        return *reinterpret_cast<const uint2*>(wsm + SM::kInBytes + ((r % SM::R) * 32 + lane) * 8);
+    auto halo_row = [&](int r, int k) -> uint2 {
+        return *reinterpret_cast<const uint2*>(wsm + SM::kInBytes + (((r % SM::RS) * R + k) * 32 + lane) * 8);
     };
-    auto u_row = [&](int i) -> uint32_t* {
-        return reinterpret_cast<uint32_t*>(wsm + SM::kUOff + (i * 32 + lane) * 16);
+    auto u_row = [&](int i, int k) -> uint32_t* {
+        return reinterpret_cast<uint32_t*>(wsm + SM::kUOff + ((i * R + k) * 32 + lane) * 16);
     };
     // In-plane terms of one level's plane: M = C | sx(C) | sy(C) [| sx(sy(C))],
     // Z = C [| sx(sy(C))]: what the plane contributes to itself and to the
     // planes above and below.
-    auto terms = [&](const uint32_t (&C)[NW], uint32_t (&M)[NW], uint32_t (&Z)[NW]) {
-        // rows: lanes 0 and 31 get their own row back from the shuffle,
-        // which is already in M, the same as an empty row outside
-        uint32_t Y[NW];
+    auto terms = [&](const uint32_t (&C)[R][NW], uint32_t (&M)[R][NW], uint32_t (&Z)[R][NW]) {
+        // rows: the lane's first row takes its upper neighbour from the
+        // previous lane's last row, its last row the lower neighbour from the
+        // next lane's first row, by shuffle; the others are in registers.
+        // Lanes 0 and 31 get their own value back from the shuffle: lane 0's
+        // last row (R = 1: the row itself, already in M; R = 2: the first
+        // row's lower neighbour, already in Y), lane 31's first row (likewise)
+        uint32_t Y[R][NW];
 #pragma unroll
-        for (int j = 0; j < NW; ++j) Y[j] = __shfl_up_sync(kFull, C[j], 1) | __shfl_down_sync(kFull, C[j], 1);
+        for (int j = 0; j < NW; ++j) {
+            const uint32_t up = __shfl_up_sync(kFull, C[R - 1][j], 1);
+            const uint32_t dn = __shfl_down_sync(kFull, C[0][j], 1);
+#pragma unroll
+            for (int k = 0; k < R; ++k) Y[k][j] = (k == 0 ? up : C[k - 1][j]) | (k == R - 1 ? dn : C[k + 1][j]);
+        }
         // x: one funnel shift per direction carries the neighbour word's
         // bit.  The words form a ring [H, I0, I1, I2, I3]: the halo word H
         // holds the left neighbour word's high half (x0 - 16 .. x0 - 1) in
@@ -307,34 +333,37 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
         // neighbour; the two halves trade bits 15 and 16, 16 voxels from the
         // interior, which T <= kTbMaxSteps (< 16) steps never carry back
 #pragma unroll
-        for (int j = 0; j < NW; ++j) {
-            const uint32_t l = C[(j + NW - 1) % NW], r = C[(j + 1) % NW];
-            const uint32_t sx = __funnelshift_l(l, C[j], 1) | __funnelshift_r(C[j], r, 1);
-            if constexpr (!SE18) {
-                M[j] = C[j] | sx | Y[j];
-                Z[j] = C[j];
-            } else {
-                const uint32_t yl = Y[(j + NW - 1) % NW], yr = Y[(j + 1) % NW];
-                const uint32_t sxy = __funnelshift_l(yl, Y[j], 1) | __funnelshift_r(Y[j], yr, 1);
-                M[j] = C[j] | sx | Y[j] | sxy;
-                Z[j] = C[j] | sxy;
+        for (int k = 0; k < R; ++k) {
+#pragma unroll
+            for (int j = 0; j < NW; ++j) {
+                const uint32_t l = C[k][(j + NW - 1) % NW], r = C[k][(j + 1) % NW];
+                const uint32_t sx = __funnelshift_l(l, C[k][j], 1) | __funnelshift_r(C[k][j], r, 1);
+                if constexpr (!SE18) {
+                    M[k][j] = C[k][j] | sx | Y[k][j];
+                    Z[k][j] = C[k][j];
+                } else {
+                    const uint32_t yl = Y[k][(j + NW - 1) % NW], yr = Y[k][(j + 1) % NW];
+                    const uint32_t sxy = __funnelshift_l(yl, Y[k][j], 1) | __funnelshift_r(Y[k][j], yr, 1);
+                    M[k][j] = C[k][j] | sx | Y[k][j] | sxy;
+                    Z[k][j] = C[k][j] | sxy;
+                }
             }
         }
     };
 
     // Per level l < T: acc = M(p) | Z(p - 1) of the pending plane p and
     // zp = Z(p); the next plane's terms complete plane p at level l + 1.
-    uint32_t acc[T][NW], zp[T][NW];
+    uint32_t acc[T][R][NW], zp[T][R][NW];
     unsigned cnt[T];
 #pragma unroll
     for (int s = 0; s < T; ++s) {
         cnt[s] = 0;
 #pragma unroll
-        for (int j = 0; j < NW; ++j) acc[s][j] = zp[s][j] = 0u;
+        for (int k = 0; k < R; ++k)
+#pragma unroll
+            for (int j = 0; j < NW; ++j) acc[s][k][j] = zp[s][k][j] = 0u;
     }
-    uint32_t d_any = 0, d_xl = 0, d_xh = 0, d_zl = 0, d_zh = 0;
-    const bool band_yl = inter && (lane - T) < T;
-    const bool band_yh = inter && (lane - T) >= BYI - T;
+    uint32_t d_xl = 0, d_xh = 0, d_zl = 0, d_zh = 0, d_yl = 0, d_yh = 0, d_any = 0;
     (void)p;
 
 #pragma unroll
@@ -344,13 +373,21 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
         if (q + SM::PF < NP) tb_copy_plane<T, BZ>(w, q + SM::PF, wsm);
         cp_async_wait_upto<SM::PF>((NP - 1 - q) < SM::PF ? (NP - 1 - q) : SM::PF);
         // level 0: the loaded plane q
-        uint32_t M[NW], Z[NW];
+        uint32_t M[R][NW], Z[R][NW];
         {
-            const uint4 v = in_row(q);
-            const uint2 h = halo_row(q);
             // zero outside the domain already (zero-fill copies, clean tail
             // bits), so no mask here
-            uint32_t C[NW] = {(h.x & 0xffff0000u) | (h.y & 0x0000ffffu), v.x, v.y, v.z, v.w};
+            uint32_t C[R][NW];
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                const uint4 v = in_row(q, k);
+                const uint2 h = halo_row(q, k);
+                C[k][0] = (h.x & 0xffff0000u) | (h.y & 0x0000ffffu);
+                C[k][1] = v.x;
+                C[k][2] = v.y;
+                C[k][3] = v.z;
+                C[k][4] = v.w;
+            }
             terms(C, M, Z);
         }
         // (M, Z) hold level s - 1 terms of plane q - s + 1: they complete
@@ -358,17 +395,19 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
 #pragma unroll
         for (int s = 1; s <= T; ++s) {
             const int r = q - s;
-            uint32_t out[NW];
+            uint32_t out[R][NW];
             // 6-neighbour element: a plane's z term is the plane itself, so
             // zp[s - 1] holds plane r at level s - 1 until it is replaced here
-            uint32_t prev[NW];
+            uint32_t prev[R][NW];
 #pragma unroll
-            for (int j = 0; j < NW; ++j) {
-                if constexpr (!SE18) prev[j] = zp[s - 1][j];
-                out[j] = acc[s - 1][j] | Z[j];
-                acc[s - 1][j] = M[j] | zp[s - 1][j];
-                zp[s - 1][j] = Z[j];
-            }
+            for (int k = 0; k < R; ++k)
+#pragma unroll
+                for (int j = 0; j < NW; ++j) {
+                    if constexpr (!SE18) prev[k][j] = zp[s - 1][k][j];
+                    out[k][j] = acc[s - 1][k][j] | Z[k][j];
+                    acc[s - 1][k][j] = M[k][j] | zp[s - 1][k][j];
+                    zp[s - 1][k][j] = Z[k][j];
+                }
             if (!(r >= s && r <= NP - 1 - s)) break;  // nothing complete at level s yet
             // Clip to the domain.  The 6-neighbour element needs it only at
             // the last level: the domain is a box and every shortest
@@ -380,41 +419,45 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
             if (SE18 || s == T) {
                 const bool pv = plane_ok(r);
 #pragma unroll
-                for (int j = 0; j < NW; ++j) out[j] = pv ? (out[j] & wm[j]) : 0u;
+                for (int k = 0; k < R; ++k)
+#pragma unroll
+                    for (int j = 0; j < NW; ++j) out[k][j] = (pv && w.rowv[k]) ? (out[k][j] & wmx[j]) : 0u;
             }
             if (r >= T && r < T + BZ) {
                 // cover test of the interior at step kb + s (target rows of
-                // non-interior lanes and planes are zero).  The state only
+                // non-interior rows and planes are zero).  The state only
                 // grows, so the voxels step kb + s covers are the target
                 // voxels in plane r at level s but not at level s - 1.
-                uint32_t* ur = u_row(r - T);
-                uint4 u = *reinterpret_cast<const uint4*>(ur);
-                if constexpr (!SE18) {
-                    u.x &= ~prev[1];
-                    u.y &= ~prev[2];
-                    u.z &= ~prev[3];
-                    u.w &= ~prev[4];
-                } else if (s == 1) {
-                    // the 18-neighbour z term is not the plane: the row keeps
-                    // the uncovered target, target minus the level-0 state
-                    const uint4 c0 = in_row(r);
-                    u.x &= ~c0.x;
-                    u.y &= ~c0.y;
-                    u.z &= ~c0.z;
-                    u.w &= ~c0.w;
-                }
-                const uint32_t h0 = out[1] & u.x, h1 = out[2] & u.y, h2 = out[3] & u.z, h3 = out[4] & u.w;
-                const uint32_t hany = h0 | h1 | h2 | h3;
-                if (hany) {
+#pragma unroll
+                for (int k = 0; k < R; ++k) {
+                    uint32_t* ur = u_row(r - T, k);
+                    uint4 u = *reinterpret_cast<const uint4*>(ur);
+                    if constexpr (!SE18) {
+                        u.x &= ~prev[k][1];
+                        u.y &= ~prev[k][2];
+                        u.z &= ~prev[k][3];
+                        u.w &= ~prev[k][4];
+                    } else if (s == 1) {
+                        // the 18-neighbour z term is not the plane: the row keeps
+                        // the uncovered target, target minus the level-0 state
+                        const uint4 c0 = in_row(r, k);
+                        u.x &= ~c0.x;
+                        u.y &= ~c0.y;
+                        u.z &= ~c0.z;
+                        u.w &= ~c0.w;
+                    }
+                    const uint32_t h0 = out[k][1] & u.x, h1 = out[k][2] & u.y, h2 = out[k][3] & u.z,
+                                   h3 = out[k][4] & u.w;
                     cnt[s - 1] += __popc(h0) + __popc(h1) + __popc(h2) + __popc(h3);
-                    u.x &= ~h0;
-                    u.y &= ~h1;
-                    u.z &= ~h2;
-                    u.w &= ~h3;
-                }
-                if constexpr (SE18) {
-                    if (s < T && (s == 1 || hany))  // the last level reads the row for the last time
-                        *reinterpret_cast<uint4*>(ur) = u;
+                    if constexpr (SE18) {
+                        if (s < T) {  // the last level reads the row for the last time
+                            u.x &= ~h0;
+                            u.y &= ~h1;
+                            u.z &= ~h2;
+                            u.w &= ~h3;
+                            *reinterpret_cast<uint4*>(ur) = u;
+                        }
+                    }
                 }
             }
             if (s < T) {
@@ -422,22 +465,28 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
             } else {
                 // final level: store, record changes
                 const int z = w.z0 - T + r;
-                if (inter && z < w.Dd) {
-                    const int off = z * bplane + browoff;
-                    const uint4 o4 = make_uint4(out[1], out[2], out[3], out[4]);
-                    *reinterpret_cast<uint4*>(dst + off) = o4;
-                    if (dst2) *reinterpret_cast<uint4*>(dst2 + off) = o4;
-                    const uint4 c0 = in_row(r);
-                    const uint32_t dx0 = out[1] ^ (c0.x & wm[1]), dx3 = out[4] ^ (c0.w & wm[4]);
-                    const uint32_t dall = dx0 | (out[2] ^ (c0.y & wm[2])) | (out[3] ^ (c0.z & wm[3])) | dx3;
-                    // only changes within T voxels of an x face can reach
-                    // the x neighbour's interior during its next T steps
-                    constexpr uint32_t kLoBits = (1u << T) - 1u, kHiBits = ~(0xffffffffu >> T);
-                    d_any |= dall;
-                    d_xl |= dx0 & kLoBits;
-                    d_xh |= dx3 & kHiBits;
-                    if (r - T < T) d_zl |= dall;
-                    if (r - T >= BZ - T) d_zh |= dall;
+#pragma unroll
+                for (int k = 0; k < R; ++k) {
+                    if (inter[k] && z < w.Dd) {
+                        const int off = z * bplane + (brow0 + k) * Jp->pitch + wx0;
+                        const uint4 o4 = make_uint4(out[k][1], out[k][2], out[k][3], out[k][4]);
+                        *reinterpret_cast<uint4*>(dst + off) = o4;
+                        if (dst2) *reinterpret_cast<uint4*>(dst2 + off) = o4;
+                        const uint4 c0 = in_row(r, k);
+                        const uint32_t dx0 = out[k][1] ^ (c0.x & wmx[1]), dx3 = out[k][4] ^ (c0.w & wmx[4]);
+                        const uint32_t dall = dx0 | (out[k][2] ^ (c0.y & wmx[2])) | (out[k][3] ^ (c0.z & wmx[3])) | dx3;
+                        // only changes within T voxels of an x face can reach
+                        // the x neighbour's interior during its next T steps
+                        constexpr uint32_t kLoBits = (1u << T) - 1u, kHiBits = ~(0xffffffffu >> T);
+                        const int yb = lane * R + k - T;  // row within the brick
+                        d_any |= dall;
+                        d_xl |= dx0 & kLoBits;
+                        d_xh |= dx3 & kHiBits;
+                        if (yb < T) d_yl |= dall;
+                        if (yb >= BYI - T) d_yh |= dall;
+                        if (r - T < T) d_zl |= dall;
+                        if (r - T >= BZ - T) d_zh |= dall;
+                    }
                 }
             }
         }
@@ -454,8 +503,8 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
     res.any = __any_sync(kFull, d_any != 0);
     res.fxl = __any_sync(kFull, d_xl != 0);
     res.fxh = __any_sync(kFull, d_xh != 0);
-    res.fyl = __any_sync(kFull, band_yl && d_any != 0);
-    res.fyh = __any_sync(kFull, band_yh && d_any != 0);
+    res.fyl = __any_sync(kFull, d_yl != 0);
+    res.fyh = __any_sync(kFull, d_yh != 0);
     res.fzl = __any_sync(kFull, d_zl != 0);
     res.fzh = __any_sync(kFull, d_zh != 0);
 }
