@@ -687,6 +687,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     sp.max_iters = kmax_all / sh.steps + 2;
     sp.stats = stats ? 1 : 0;
     sp.spread = sh.spread;
+    sp.job_cache = (n == 1 && sh.kernel == 2) ? hdk::kJobCache : 0;  // a single pair's two jobs
     sp.timeout_ns = ctx->opt.barrier_timeout_ns > 0 ? ctx->opt.barrier_timeout_ns : 10000000000LL;
     const int occ = occupancy_of(ctx, solve_fn, sh.threads, sh.smem);
     if (occ <= 0) return set_error(ctx, HD_ERR_CUDA, "dilation kernel cannot be made resident");

@@ -169,13 +169,14 @@ __device__ __forceinline__ void tb_copy_plane(const TbRow<tb_rows(T)>& w, int r,
 // batch, so their latencies overlap; the flag is checked when the item is
 // computed.
 template <int T>
-__device__ __forceinline__ bool tb_decode(const SolveParams& p, unsigned long long e, int g, TbItem& it) {
+__device__ __forceinline__ bool tb_decode(const SolveParams& p, unsigned long long e, int g, const Job* jcache,
+                                          TbItem& it) {
     const int lane = threadIdx.x & 31;
     it.jid = (int)((e >> 32) & 0xffffffu);
     it.lb = (unsigned)e;
     it.epoch = (unsigned)(e >> 56);
     it.st = p.states + it.jid;
-    it.Jp = p.jobs + it.jid;
+    it.Jp = it.jid < p.job_cache ? jcache + it.jid : p.jobs + it.jid;
     it.live = false;
     const Job* Jp = it.Jp;
     // the job's active flag is only needed when the item is computed: the
@@ -210,11 +211,12 @@ __device__ __forceinline__ bool tb_decode(const SolveParams& p, unsigned long lo
 // target rows (one group) and of its first planes (one group each).  No
 // wait.
 template <int T, int BZ>
-__device__ __forceinline__ void tb_issue(const SolveParams& p, unsigned long long e, int g, unsigned char* wsm,
+__device__ __forceinline__ void tb_issue(const SolveParams& p, unsigned long long e, int g, const Job* jcache,
+                                         unsigned char* wsm,
                                          TbItem& it) {
     using SM = TbSmem<T, BZ>;
     const int lane = threadIdx.x & 31;
-    if (!tb_decode<T>(p, e, g, it)) return;
+    if (!tb_decode<T>(p, e, g, jcache, it)) return;
     {
         const TbRow<SM::R> t = tb_row<T, BZ>(it, true);
         const uint32_t s_u = (uint32_t)__cvta_generic_to_shared(wsm) + SM::kUOff;
@@ -574,11 +576,16 @@ __global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel
     extern __shared__ __align__(16) unsigned char tb_smem[];
     __shared__ int s_flag;
     __shared__ unsigned s_gen, s_cnt;
+    __shared__ Job s_jobs[kJobCache];
     Ctl* ctl = p.ctl;
     if (threadIdx.x == 0) {
         s_gen = (unsigned)(ld_acquire_u64(&ctl->release) >> 32);
         s_cnt = ld_relaxed_u32(&ctl->qcount[p.g0 % 3]);
     }
+    // the first line of each cached job (every field an item reads)
+    if (threadIdx.x < 32 * p.job_cache)
+        reinterpret_cast<uint32_t*>(&s_jobs[threadIdx.x >> 5])[threadIdx.x & 31] =
+            reinterpret_cast<const uint32_t*>(p.jobs + (threadIdx.x >> 5))[threadIdx.x & 31];
     __syncthreads();
     unsigned gen = s_gen;
     unsigned cnt = s_cnt;
@@ -599,7 +606,7 @@ __global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel
             TbItem cur;
             cur.live = false;
             unsigned i = gw;
-            if (i < cnt) tb_issue<T, BZ>(p, Q[i], g, wsm, cur);
+            if (i < cnt) tb_issue<T, BZ>(p, Q[i], g, s_jobs, wsm, cur);
             while (i < cnt) {
                 const unsigned in = i + nw;
                 const unsigned long long en = in < cnt ? Q[in] : 0ull;
@@ -607,7 +614,7 @@ __global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel
                 if (cur.live) tb_compute<T, BZ, SE18>(p, cur, wsm, res);
                 TbItem nxt;
                 nxt.live = false;
-                if (in < cnt) tb_issue<T, BZ>(p, en, g, wsm, nxt);
+                if (in < cnt) tb_issue<T, BZ>(p, en, g, s_jobs, wsm, nxt);
                 if (cur.live) tb_epilogue<T, SE18>(p, cur, res, g);
                 cur = nxt;
                 i = in;
