@@ -15,8 +15,10 @@
 //                     voxels in a step's result but not in its input)
 //               domain layout [z][y][pitch] words, pitch = ceil(wx / 4) * 4,
 //               pad words zero.  The domain is the bounding box of A u B with
-//               x widened to whole words (6-neighbour element) or the whole
-//               volume (18-neighbour element).  The blocked kernel reads its
+//               x widened to whole words (6-neighbour element), widened by
+//               one more word in x and one row and plane in y and z
+//               (18-neighbour element: shortest paths may step one voxel
+//               out of the box, see domain_box).  The blocked kernel reads its
 //               first iteration's state and the target from the packed
 //               masks in place when the domain can start on a multiple of 4
 //               words without adding a brick column; else from crops of A

@@ -355,32 +355,51 @@ struct Domain {
     int ox, oy, oz, wv, h, d, wx0, wx, pitch;
 };
 
-__device__ __forceinline__ Domain make_domain(const PairDesc& P, const PairInfo& I, bool quad) {
-    Domain m;
-    if (P.se == 0) {
-        // 6-neighbour element: every shortest path between two voxels of the
-        // bounding box of A u B is monotone and stays in it, so cropping to it
-        // (or to any box inside the volume that contains it: x widened to
-        // whole words, or to a start on a multiple of 4 words when `quad`)
-        // is exact.
-        m.wx0 = quad ? (I.bb[0] & ~3) : I.bb[0];  // word columns
-        const int wx1 = I.bb[1];
-        m.ox = 32 * m.wx0;
-        m.wv = min(P.W, 32 * (wx1 + 1)) - m.ox;
-        m.oy = I.bb[2];
-        m.h = I.bb[3] - I.bb[2] + 1;
-        m.oz = I.bb[4];
-        m.d = I.bb[5] - I.bb[4] + 1;
-    } else {
-        // 18-neighbour element: shortest paths may step outside the box
-        // (e.g. (1,1,1)+(1,-1,1) reaches (2,0,2) in 2 steps), so the domain
-        // is the whole volume, as in the reference.
-        m.wx0 = 0;
-        m.ox = m.oy = m.oz = 0;
-        m.wv = P.W;
-        m.h = P.H;
-        m.d = P.D;
+// Bounding box of the domain, before any rounding of its first word: the
+// 6-neighbour element uses the bounding box of A u B (x in whole words), the
+// 18-neighbour element that box widened by one word in x and one row and
+// plane in y and z, clipped to the volume.  Exactness: a shortest
+// 6-neighbour path between two voxels of a box is monotone and stays in it.
+// An 18-neighbour step (the 6 face neighbours, the 4 in-plane diagonals and
+// the 8 corners) changes z by at most 1 and x and y together through the
+// corners; between two voxels at offsets (a, b, c) a shortest path takes c
+// z steps whose corners' x and y moves alternate around the needed offset,
+// plus king moves in the plane, so it leaves the box of the two voxels by
+// at most one voxel in x or y and never in z (where it would need two more
+// z steps).  Where the widened box is clipped by the volume, the whole
+// volume offers no detour on that side either.  (Without the margin the
+// results differ: offset (0, 2, 2) takes the corners (1, 1, 1) and
+// (-1, 1, 1), 2 steps, against 4 inside a box one voxel wide in x.)
+struct DomainBox {
+    int w0, w1, y0, y1, z0, z1;  // inclusive: word columns, rows, planes
+};
+__device__ __forceinline__ DomainBox domain_box(const PairDesc& P, const PairInfo& I) {
+    DomainBox b{I.bb[0], I.bb[1], I.bb[2], I.bb[3], I.bb[4], I.bb[5]};
+    if (P.se != 0) {
+        const int wxf = (P.W + 31) >> 5;
+        b.w0 = max(0, b.w0 - 1);
+        b.w1 = min(wxf - 1, b.w1 + 1);
+        b.y0 = max(0, b.y0 - 1);
+        b.y1 = min(P.H - 1, b.y1 + 1);
+        b.z0 = max(0, b.z0 - 1);
+        b.z1 = min(P.D - 1, b.z1 + 1);
     }
+    return b;
+}
+
+// The domain of a pair (quad: its first word rounded down to a multiple of
+// 4, so that its rows start on 16-byte boundaries of the packed masks; any
+// box inside the volume that contains the one above is as exact).
+__device__ __forceinline__ Domain make_domain(const PairDesc& P, const PairInfo& I, bool quad) {
+    const DomainBox b = domain_box(P, I);
+    Domain m;
+    m.wx0 = quad ? (b.w0 & ~3) : b.w0;  // word columns
+    m.ox = 32 * m.wx0;
+    m.wv = min(P.W, 32 * (b.w1 + 1)) - m.ox;
+    m.oy = b.y0;
+    m.h = b.y1 - b.y0 + 1;
+    m.oz = b.z0;
+    m.d = b.z1 - b.z0 + 1;
     m.wx = (m.wv + 31) >> 5;
     m.pitch = (m.wx + 3) & ~3;
     return m;
@@ -388,12 +407,11 @@ __device__ __forceinline__ Domain make_domain(const PairDesc& P, const PairInfo&
 
 // Blocked kernel: can the domain start on a multiple of 4 words (its rows
 // then start on 16-byte boundaries of the packed masks, which the kernel
-// reads in place) without adding a brick column?  The 18-neighbour domain
-// is the whole volume, which starts at word 0.
+// reads in place) without adding a brick column?
 __device__ __forceinline__ bool blocked_in_place(const PairDesc& P, const PairInfo& I) {
-    if (P.se != 0) return true;
-    const int w1 = I.bb[1] + 1;  // the domain's words end here (inside the volume)
-    return (w1 - I.bb[0] + 3) / 4 == (w1 - (I.bb[0] & ~3) + 3) / 4;
+    const DomainBox b = domain_box(P, I);
+    const int w1 = b.w1 + 1;  // the domain's words end here (inside the volume)
+    return (w1 - b.w0 + 3) / 4 == (w1 - (b.w0 & ~3) + 3) / 4;
 }
 
 __device__ __forceinline__ long long setup_tile(const PairDesc& P, long long tile_in_pair, Job* jobs,

@@ -416,8 +416,9 @@ __device__ __forceinline__ void tb_compute(const SolveParams& p, const TbItem& i
             // 6-neighbour path between two of its voxels stays inside it, so
             // dilating past its faces for a few levels changes nothing inside
             // (and the target words are zero outside).  The
-            // 18-neighbour element's paths can leave and re-enter the box: it
-            // is clipped at every level, like the reference's border guards.
+            // 18-neighbour element's paths can leave and re-enter a box (its
+            // domain has a margin for that): it is clipped at every level,
+            // like the reference's border guards.
             if (SE18 || s == T) {
                 const bool pv = plane_ok(r);
 #pragma unroll

@@ -237,13 +237,13 @@ def test_profile_tile_counts(ctx, oracle, metric):
     o = oracle.bfs_pair(a, b, metric)
     assert_same(g, o)
     D, H, W = a.shape
-    if metric == "se6":
-        zz, yy, xx = np.nonzero(a | b)
-        x0 = (xx.min() // 32) * 32
-        x1 = min(W - 1, (xx.max() // 32) * 32 + 31)
-        box = (x0, x1, yy.min(), yy.max(), zz.min(), zz.max())
-    else:
-        box = (0, W - 1, 0, H - 1, 0, D - 1)
+    # the domain: the bounding box of A u B, x in whole words; the
+    # 18-neighbour element widens it by a word, a row and a plane
+    zz, yy, xx = np.nonzero(a | b)
+    m = 0 if metric == "se6" else 1
+    w0, w1 = max(0, xx.min() // 32 - m), min((W - 1) // 32, xx.max() // 32 + m)
+    box = (32 * w0, min(W - 1, 32 * w1 + 31), max(0, yy.min() - m), min(H - 1, yy.max() + m),
+           max(0, zz.min() - m), min(D - 1, zz.max() + m))
     da = oracle.bfs_dt(a, metric)
     db = oracle.bfs_dt(b, metric)
     want_ba = oracle.tile_counts(da, box, g["hd_ba"])
@@ -516,3 +516,43 @@ def test_prepared_batch_columns_equal_batch(hd, ctx):
             for k in KEYS:
                 assert got[i][k] == w[k] and int(cols[k][i]) == w[k], (i, k)
     assert ctx.prepare_batch([], "se6").run(columns=True)["hd"].shape == (0,)
+
+
+@pytest.mark.parametrize("kernel", [1, 2])
+def test_se18_paths_that_leave_the_bounding_box(hd, oracle, kernel):
+    """The 18-neighbour element's shortest paths may step one voxel out of
+    the bounding box of A u B (offset (0, 2, 2) takes the corners (1, 1, 1)
+    and (-1, 1, 1)); the CUDA path's domain keeps that margin.  Single voxels
+    at such offsets in the middle of the volume, against its faces (where the
+    volume clips the margin) and in its corners, thin diagonal lines: every
+    field against the oracle's transforms over the whole volume."""
+    rng = np.random.default_rng(23)
+    cases = []
+    V = (12, 40, 70)  # D, H, W: x spans three words
+    for (dz, dy, dx) in [(0, 2, 2), (2, 0, 2), (2, 2, 0), (0, 3, 3), (3, 1, 0), (1, 0, 3), (2, 1, 1), (4, 0, 0),
+                         (0, 0, 4), (3, 3, 1)]:
+        for (z, y, x) in [(5, 20, 35), (0, 0, 0), (0, 20, 31), (5, 0, 32), (10, 38, 64), (7, 39, 69)]:
+            zb, yb, xb = z + dz, y + dy, x + dx
+            if not (0 <= zb < V[0] and 0 <= yb < V[1] and 0 <= xb < V[2]):
+                zb, yb, xb = z - dz, y - dy, x - dx
+            if not (0 <= zb < V[0] and 0 <= yb < V[1] and 0 <= xb < V[2]):
+                continue
+            a = np.zeros(V, np.uint8)
+            b = np.zeros(V, np.uint8)
+            a[z, y, x] = 1
+            b[zb, yb, xb] = 1
+            cases.append((a, b))
+    for _ in range(12):
+        a = np.zeros(V, np.uint8)
+        b = np.zeros(V, np.uint8)
+        for m in (a, b):
+            z, y, x = (int(rng.integers(0, s)) for s in V)
+            sz, sy = int(rng.integers(-1, 2)), int(rng.integers(-1, 2))
+            for t in range(int(rng.integers(1, 9))):
+                if 0 <= z + sz * t < V[0] and 0 <= y + sy * t < V[1]:
+                    m[z + sz * t, y + sy * t, x] = 1
+        cases.append((a, b))
+    with hd.Context(0, kernel=kernel) as kctx:
+        for i, (a, b) in enumerate(cases):
+            o = oracle.bfs_pair(a, b, "se18")
+            assert_same(kctx.compute(cuda(a), cuda(b), "se18"), o, f"case {i} kernel {kernel}")

@@ -113,3 +113,62 @@ def test_tile_counts(oracle):
     assert list(t) == [0, 1, 1, 1]
     t = oracle.tile_counts(d, (0, 69, 0, 39, 0, 39), 40)
     assert t[32] == 4  # distance 32 reaches the x, y and z neighbour tiles and stays in the first
+
+
+def _crop_margin(a, b, mx, my, mz):
+    """The masks on the bounding box of A u B widened by (mx, my, mz) voxels,
+    clipped to the volume."""
+    u = (a != 0) | (b != 0)
+    zz, yy, xx = (np.where(u.any(axis=ax))[0] for ax in ((1, 2), (0, 2), (0, 1)))
+    D, H, W = a.shape
+    sl = (slice(max(0, zz[0] - mz), min(D, zz[-1] + 1 + mz)), slice(max(0, yy[0] - my), min(H, yy[-1] + 1 + my)),
+          slice(max(0, xx[0] - mx), min(W, xx[-1] + 1 + mx)))
+    return a[sl].copy(), b[sl].copy()
+
+
+def _same_pair_result(r, q):
+    keys = ("hd", "hd_ab", "hd_ba", "sum_ab", "sum_ba", "n_a", "n_b", "n_a_not_b", "n_b_not_a", "status")
+    if any(r[k] != q[k] for k in keys):
+        return False
+    for h in ("hist_ab", "hist_ba"):
+        n = min(len(r[h]), len(q[h]))
+        if not np.array_equal(r[h][:n], q[h][:n]) or r[h][n:].any() or q[h][n:].any():
+            return False
+    return True
+
+
+def test_se18_domain_margin(oracle):
+    """The 18-neighbour domain of the CUDA path is the bounding box of A u B
+    widened by one voxel in x and y (the path widens x by a whole word and z
+    by a plane as well): on it the breadth-first transforms give the same
+    results and per-step histograms as on the whole volume, while the bare
+    bounding box does not (a shortest path may step one voxel out of it)."""
+    rng = np.random.default_rng(11)
+    bare_differs = 0
+    cases = 0
+    V = 16
+    for dz in range(-4, 5):
+        for dy in range(-4, 5):
+            for dx in range(-4, 5):
+                a = np.zeros((V, V, V), np.uint8)
+                b = np.zeros_like(a)
+                a[8, 8, 8] = 1
+                b[8 + dz, 8 + dy, 8 + dx] = 1
+                full = oracle.bfs_pair(a, b, "se18", hist=True)
+                assert _same_pair_result(full, oracle.bfs_pair(*_crop_margin(a, b, 1, 1, 0), "se18", hist=True)), \
+                    (dz, dy, dx)
+                bare_differs += not _same_pair_result(full, oracle.bfs_pair(*_crop_margin(a, b, 0, 0, 0), "se18",
+                                                                              hist=True))
+                cases += 1
+    for _ in range(60):
+        shape = tuple(int(v) for v in rng.integers(5, 20, size=3))
+        p = float(rng.choice([0.003, 0.02, 0.1]))
+        a = (rng.random(shape) < p).astype(np.uint8)
+        b = (rng.random(shape) < p).astype(np.uint8)
+        if not (a.any() and b.any()):
+            continue
+        full = oracle.bfs_pair(a, b, "se18", hist=True)
+        for m in ((1, 1, 0), (1, 1, 1), (32, 1, 1)):
+            assert _same_pair_result(full, oracle.bfs_pair(*_crop_margin(a, b, *m), "se18", hist=True)), (shape, m)
+        cases += 1
+    assert bare_differs > 0  # the margin is needed
