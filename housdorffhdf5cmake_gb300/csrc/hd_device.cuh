@@ -224,10 +224,13 @@ struct SolveParams {
     // at the next grid barrier (null: never)
     const int32_t* yield;
     int32_t yield_gen;
-    // blocked kernel: jobs 0 .. job_cache - 1 (at most kJobCache) are read
-    // from a per-CTA copy of their first line, taken at the start of the
-    // launch (no kernel writes a job while the dilation runs); 0: none
+    // blocked kernel: jobs job_cache_base .. job_cache_base + job_cache - 1
+    // (at most kJobCache: a single pair, or a server tick with one resident
+    // request) are read from a per-CTA copy of their first line, taken at the
+    // start of the launch (no kernel writes a job while the dilation runs);
+    // job_cache 0: none
     int32_t job_cache;
+    int32_t job_cache_base;
 };
 constexpr int kJobCache = 2;
 

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -169,6 +170,12 @@ struct hd_server {
     hd_server_stats stats{};
     std::string err;
     bool debug = false;  // HD_SERVER_DEBUG=1: one line per tick on stderr
+    // Advanced (under the lock) by every submission, cancel and stop
+    // (wake_seq) and by every completion (done_seq): the worker's idle poll
+    // and the waiters' spin read them without the lock, which they take only
+    // when a count has moved, so the polls do not compete with the tick and
+    // with submissions for the lock.
+    std::atomic<unsigned long long> wake_seq{0}, done_seq{0};
 };
 
 namespace {
@@ -204,6 +211,7 @@ void plan_request(hd_server* s, Request* r) {
 // Marks a request done (server lock held) and lists it for wait_any.
 void mark_done(hd_server* s, Request* r) {
     r->state = kDone;
+    s->done_seq.fetch_add(1, std::memory_order_release);
     // tickets taken by poll / wait leave the completion list from its front
     while (!s->done_order.empty() && !s->reqs.count(s->done_order.front())) s->done_order.pop_front();
     s->done_order.push_back(r->ticket);
@@ -420,6 +428,16 @@ void tick(hd_server* s) {
         sp.decode_done_only = 1;
         sp.yield = s->d_yield;
         sp.yield_gen = ygen;
+        if (resident == 1 && s->shape.kernel == 2) {
+            // a lone request: its two jobs are read from a per-CTA copy (the
+            // jobs change only between ticks: set-up and retire run on this
+            // stream before the launch)
+            for (size_t i = 0; i < s->slots.size(); ++i)
+                if (s->slots[i]) {
+                    sp.job_cache = hdk::kJobCache;
+                    sp.job_cache_base = 2 * (int32_t)i;
+                }
+        }
         void* args[] = {&sp};
         // yield words posted before this tick have landed
         e = cudaStreamWaitEvent(st, s->ev_yield, 0);
@@ -580,10 +598,19 @@ void worker_main(hd_server* s) {
     for (;;) {
         // idle: poll for a new request for a short while before sleeping
         // (a wake-up through the condition variable costs tens of
-        // microseconds of a request's latency)
+        // microseconds of a request's latency); the lock is taken only when
+        // a submission, cancel or stop has moved wake_seq
         const auto t_idle = std::chrono::steady_clock::now();
+        unsigned long long seen = s->wake_seq.load(std::memory_order_acquire);
         bool work = false;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            work = has_work();
+        }
         while (!work && std::chrono::steady_clock::now() - t_idle < std::chrono::microseconds(kIdleSpinUs)) {
+            const unsigned long long now_seq = s->wake_seq.load(std::memory_order_acquire);
+            if (now_seq == seen) continue;
+            seen = now_seq;
             std::lock_guard<std::mutex> lk(s->mu);
             work = has_work();
         }
@@ -596,19 +623,28 @@ void worker_main(hd_server* s) {
     }
 }
 
-// Polls `ready` (server lock held by `lk`, released between polls) for up
-// to kWaitSpinUs, or timeout_ms if that is shorter; true once it holds.  A
-// result that lands within the window is picked up without the
-// condition variable's wake-up latency.
+// Polls `ready` (server lock held by `lk`) for up to kWaitSpinUs, or
+// timeout_ms if that is shorter; true once it holds.  Between checks the
+// lock is released and only the completion count is read, without the
+// lock, until it moves.  A result that lands within the window is picked up
+// without the condition variable's wake-up latency.
 template <class F>
-bool spin_wait(std::unique_lock<std::mutex>& lk, F ready, int64_t timeout_ms) {
+bool spin_wait(hd_server* s, std::unique_lock<std::mutex>& lk, F ready, int64_t timeout_ms) {
     const auto lim = std::chrono::microseconds(
         timeout_ms >= 0 ? std::min<int64_t>(kWaitSpinUs, timeout_ms * 1000) : kWaitSpinUs);
     const auto t0 = std::chrono::steady_clock::now();
     while (!ready()) {
-        if (std::chrono::steady_clock::now() - t0 >= lim) return false;
+        const unsigned long long seen = s->done_seq.load(std::memory_order_acquire);
         lk.unlock();
+        bool timed_out = false;
+        while (s->done_seq.load(std::memory_order_acquire) == seen) {
+            if (std::chrono::steady_clock::now() - t0 >= lim) {
+                timed_out = true;
+                break;
+            }
+        }
         lk.lock();
+        if (timed_out) return ready();
     }
     return true;
 }
@@ -770,6 +806,7 @@ hd_status hd_server_submit(hd_server* s, const hd_pair_desc* pair, uint64_t* tic
         if (e == cudaSuccess) e = cudaEventRecord(s->ev_yield, s->side);
         if (e != cudaSuccess) cudaGetLastError();  // the tick then simply runs to its end
     }
+    s->wake_seq.fetch_add(1, std::memory_order_release);
     s->cv.notify_all();
     return HD_OK;
 }
@@ -792,7 +829,7 @@ hd_status hd_server_wait(hd_server* s, uint64_t ticket, int64_t timeout_ms, hd_r
     if (it == s->reqs.end()) return HD_ERR_BAD_ARG;
     Request* r = it->second.get();
     auto ready = [&] { return r->state == kDone; };
-    spin_wait(lk, ready, timeout_ms);
+    spin_wait(s, lk, ready, timeout_ms);
     if (timeout_ms < 0) {
         s->done_cv.wait(lk, ready);
     } else if (!s->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
@@ -811,7 +848,7 @@ hd_status hd_server_wait_any(hd_server* s, int64_t timeout_ms, uint64_t* ticket,
         while (!s->done_order.empty() && !s->reqs.count(s->done_order.front())) s->done_order.pop_front();
         if (!s->done_order.empty()) break;
         auto ready = [&] { return !s->done_order.empty(); };
-        if (spin_wait(lk, ready, timeout_ms)) continue;
+        if (spin_wait(s, lk, ready, timeout_ms)) continue;
         if (timeout_ms < 0) {
             s->done_cv.wait(lk, ready);
         } else if (!s->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
@@ -833,6 +870,7 @@ hd_status hd_server_cancel(hd_server* s, uint64_t ticket) {
     if (it == s->reqs.end()) return HD_ERR_BAD_ARG;
     if (it->second->state == kDone) return HD_OK;
     it->second->cancel = true;
+    s->wake_seq.fetch_add(1, std::memory_order_release);
     s->cv.notify_all();
     return HD_OK;
 }
@@ -853,6 +891,7 @@ hd_status hd_server_destroy(hd_server* s) {
     {
         std::lock_guard<std::mutex> lk(s->mu);
         s->stop = true;
+        s->wake_seq.fetch_add(1, std::memory_order_release);
         s->cv.notify_all();
     }
     if (s->worker.joinable()) s->worker.join();

@@ -176,7 +176,8 @@ __device__ __forceinline__ bool tb_decode(const SolveParams& p, unsigned long lo
     it.lb = (unsigned)e;
     it.epoch = (unsigned)(e >> 56);
     it.st = p.states + it.jid;
-    it.Jp = it.jid < p.job_cache ? jcache + it.jid : p.jobs + it.jid;
+    const unsigned jc = (unsigned)(it.jid - p.job_cache_base);
+    it.Jp = jc < (unsigned)p.job_cache ? jcache + jc : p.jobs + it.jid;
     it.live = false;
     const Job* Jp = it.Jp;
     // the job's active flag is only needed when the item is computed: the
@@ -586,7 +587,7 @@ __global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel
     // the first line of each cached job (every field an item reads)
     if (threadIdx.x < 32 * p.job_cache)
         reinterpret_cast<uint32_t*>(&s_jobs[threadIdx.x >> 5])[threadIdx.x & 31] =
-            reinterpret_cast<const uint32_t*>(p.jobs + (threadIdx.x >> 5))[threadIdx.x & 31];
+            reinterpret_cast<const uint32_t*>(p.jobs + p.job_cache_base + (threadIdx.x >> 5))[threadIdx.x & 31];
     __syncthreads();
     unsigned gen = s_gen;
     unsigned cnt = s_cnt;
