@@ -101,9 +101,11 @@ inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
 // How long the scheduler polls for new requests when it runs out of work
 // before it sleeps on the condition variable, and how long hd_server_wait /
-// hd_server_wait_any poll before they sleep.
-constexpr int kIdleSpinUs = 500;
-constexpr int kWaitSpinUs = 200;
+// hd_server_wait_any poll before they sleep (a wake-up through the
+// condition variable adds tens of microseconds to a request's latency; the
+// polls read one atomic count, not the server lock).
+constexpr int kIdleSpinUs = 2000;
+constexpr int kWaitSpinUs = 1000;
 // Busy periods: single-pair kernel shape when at most kFewRequests wait as
 // the server starts work; batch shape after a drain once more than
 // kQueueForBatchMode wait.
