@@ -4,23 +4,29 @@
 // Same job model, queues, stamps, ping-pong buffers and barrier as
 // hd_solve.cuh, but one queue item advances a brick by T dilation steps:
 //
-//   brick     IW = 4 words (128 voxels) in x  x  32 - 2T rows  x  BZ planes
-//   warp      lane = one row: the 4 interior words plus one halo word
-//             holding the 16 voxels on each side of them, rows y0 - T ..
-//             y0 + 32 - T - 1 (T halo rows above and below the interior),
-//             streamed plane by plane along z from z0 - T to z0 + BZ + T - 1
+//   brick     IW = 4 words (128 voxels) in x  x  32 R - 2T rows  x  BZ
+//             planes, R = tb_rows(T) rows per lane (1 in this build)
+//   warp      lane = R consecutive rows: per row the 4 interior words plus
+//             one halo word holding the 16 voxels on each side of them, rows
+//             y0 - T .. y0 + 32 R - T - 1 (T halo rows above and below the
+//             interior), streamed plane by plane along z from z0 - T to
+//             z0 + BZ + T - 1
 //   levels    level 0 is the loaded state; level s is the state after s
 //             steps, computed one plane behind level s - 1 from three of its
-//             planes; rows come from the neighbouring lanes by shuffle, x
+//             planes; rows come from the lane's own registers and, for its
+//             first and last row, from the neighbouring lanes by shuffle; x
 //             carries from the neighbouring words of the row
 //   staging   planes arrive by cp.async (zero fill outside the domain) in
 //             a ring of shared-memory slots two planes ahead of the one
 //             being computed; a plane leaves the ring after its final step
 //             has been compared with it.  Per level the lane keeps the
 //             pending plane's partial result and the last plane's z terms in
-//             registers (3 CTAs of 4 warps per SM)
+//             registers (3 CTAs of 4 warps per SM; 4 for 1-2 steps)
+//   jobs      a launch with at most kJobCache jobs in play (a single pair, a
+//             server tick with one resident request) reads them from a
+//             per-CTA shared-memory copy of their first line
 //
-// Level s is exact on rows [s, 32 - s) and planes [s, BZ + 2T - s) of the
+// Level s is exact on rows [s, 32 R - s) and planes [s, BZ + 2T - s) of the
 // streamed block (errors from the unknown outside creep in one voxel per
 // step; the halo word absorbs x for T < 16), so the interior is exact for all
 // s <= T.  At every level the interior is cover-tested (hits are counted with
