@@ -194,7 +194,10 @@ struct Ctl {
     unsigned int qcount[3];
     int32_t g_end;         // next global iteration (written at exit)
     int32_t iters_run;
-    int32_t pad[6];
+    // blocked kernel: items of a step's queue handed out past its static
+    // share (per step modulo 3; the barrier zeroes the next step's count)
+    unsigned int claim[3];
+    int32_t pad[3];
 };
 
 struct SolveParams {

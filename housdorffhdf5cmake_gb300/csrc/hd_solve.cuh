@@ -98,6 +98,7 @@ __device__ __forceinline__ bool grid_step_barrier(Ctl* ctl, unsigned& gen, int g
             const bool yl = yield != nullptr && ld_relaxed_s32(yield) != yield_gen;
             const bool cont = err == 0 && jobs > 0 && nq > 0u && !yl;
             ctl->qcount[(g + 2) % 3] = 0u;
+            ctl->claim[(g + 1) % 3] = 0u;  // nobody claims from the next step's queue yet
             rel = ((unsigned long long)target << 32) | (cont ? 0x80000000ull : 0ull) | (nq & 0x7fffffffu);
             atom_exch_release_u64(&ctl->release, rel);
         } else {

@@ -248,6 +248,7 @@ __device__ __forceinline__ void tb_issue(const SolveParams& p, unsigned long lon
 
 // What the epilogue of an item needs from its compute phase.
 constexpr int kTbMaxSteps = 5;
+constexpr unsigned kTbClaimRounds = 4;  // items per warp from which the queue's tail is claimed
 struct TbOut {
     unsigned cnt[kTbMaxSteps];  // newly covered voxels per step of the item
     bool any, fxl, fxh, fyl, fyh, fzl, fzh;
@@ -609,14 +610,30 @@ __global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel
         for (;;) {
             const int qi = g % 3;
             const unsigned long long* Q = qi == 0 ? p.queue[0] : (qi == 1 ? p.queue[1] : p.queue[2]);
+            // Items to warps: with at least kTbClaimRounds items per warp,
+            // the first three quarters of the queue go to the warps by a
+            // static stride and the rest one at a time from a counter, to
+            // whichever warp is free first (warps with the same number of
+            // items finish up to a fifth apart); each claim is issued one
+            // item ahead, so its round trip overlaps the brick in between.
+            // Fewer items: the static stride only.
+            const unsigned rounds = cnt / nw;
+            const unsigned S = rounds >= kTbClaimRounds ? (rounds - rounds / 4) * nw : cnt;
+            unsigned* claimp = &ctl->claim[g % 3];
+            unsigned c_next = 0u;
             // two-stage pipeline per warp: the next brick's copies are in
             // flight while this brick's epilogue atomics run
             TbItem cur;
             cur.live = false;
             unsigned i = gw;
+            // a claim precedes every dynamic next item: the first one here
+            // when the warp's static share is its first item alone
+            if (S < cnt && i < cnt && i + nw >= S && (threadIdx.x & 31) == 0) c_next = atomicAdd(claimp, 1u);
             if (i < cnt) tb_issue<T, BZ>(p, Q[i], g, s_jobs, wsm, cur);
             while (i < cnt) {
-                const unsigned in = i + nw;
+                unsigned in = i + nw;
+                if (in >= S && S < cnt) in = S + __shfl_sync(kFull, c_next, 0);  // claimed one item ago
+                if (S < cnt && in < cnt && in + nw >= S && (threadIdx.x & 31) == 0) c_next = atomicAdd(claimp, 1u);
                 const unsigned long long en = in < cnt ? Q[in] : 0ull;
                 TbOut res;
                 if (cur.live) tb_compute<T, BZ, SE18>(p, cur, wsm, res);
