@@ -610,33 +610,43 @@ __global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel
         for (;;) {
             const int qi = g % 3;
             const unsigned long long* Q = qi == 0 ? p.queue[0] : (qi == 1 ? p.queue[1] : p.queue[2]);
-            // Items to warps: with at least kTbClaimRounds items per warp,
-            // the first three quarters of the queue go to the warps by a
-            // static stride and the rest one at a time from a counter, to
-            // whichever warp is free first (warps with the same number of
-            // items finish up to a fifth apart); each claim is issued one
-            // item ahead, so its round trip overlaps the brick in between.
-            // Fewer items: the static stride only.
+            // Items to warps: a static stride (warp w takes entries w,
+            // w + warps, ...) for the first part of the queue, the rest one
+            // at a time from a counter, to whichever warp is free first
+            // (warps with the same number of items finish up to a fifth
+            // apart).  With at least kTbClaimRounds items per warp the last
+            // quarter is claimed, each claim issued one item ahead so that
+            // its round trip overlaps the brick in between; with fewer, the
+            // entries past the last full stride are claimed after a warp's
+            // last static brick (its round trip then waits, for those items
+            // only, but they go to the warps that finished first).
             const unsigned rounds = cnt / nw;
-            const unsigned S = rounds >= kTbClaimRounds ? (rounds - rounds / 4) * nw : cnt;
+            const bool ahead = rounds >= kTbClaimRounds;
+            const unsigned S = ahead ? (rounds - rounds / 4) * nw : (rounds > 0 ? rounds * nw : cnt);
             unsigned* claimp = &ctl->claim[g % 3];
+            const bool lane0 = (threadIdx.x & 31) == 0;
             unsigned c_next = 0u;
             // two-stage pipeline per warp: the next brick's copies are in
             // flight while this brick's epilogue atomics run
             TbItem cur;
             cur.live = false;
             unsigned i = gw;
-            // a claim precedes every dynamic next item: the first one here
-            // when the warp's static share is its first item alone
-            if (S < cnt && i < cnt && i + nw >= S && (threadIdx.x & 31) == 0) c_next = atomicAdd(claimp, 1u);
+            // ahead: a claim precedes every dynamic next item, the first one
+            // here when the warp's static share is its first item alone
+            if (ahead && S < cnt && i < cnt && i + nw >= S && lane0) c_next = atomicAdd(claimp, 1u);
             if (i < cnt) tb_issue<T, BZ>(p, Q[i], g, s_jobs, wsm, cur);
             while (i < cnt) {
                 unsigned in = i + nw;
-                if (in >= S && S < cnt) in = S + __shfl_sync(kFull, c_next, 0);  // claimed one item ago
-                if (S < cnt && in < cnt && in + nw >= S && (threadIdx.x & 31) == 0) c_next = atomicAdd(claimp, 1u);
-                const unsigned long long en = in < cnt ? Q[in] : 0ull;
+                const bool late = !ahead && in >= S && S < cnt;  // claimed after this brick
+                if (ahead && in >= S && S < cnt) in = S + __shfl_sync(kFull, c_next, 0);  // claimed one item ago
+                if (ahead && S < cnt && in < cnt && in + nw >= S && lane0) c_next = atomicAdd(claimp, 1u);
+                unsigned long long en = (!late && in < cnt) ? Q[in] : 0ull;
                 TbOut res;
                 if (cur.live) tb_compute<T, BZ, SE18>(p, cur, wsm, res);
+                if (late) {
+                    in = S + __shfl_sync(kFull, lane0 ? atomicAdd(claimp, 1u) : 0u, 0);
+                    en = in < cnt ? Q[in] : 0ull;
+                }
                 TbItem nxt;
                 nxt.live = false;
                 if (in < cnt) tb_issue<T, BZ>(p, en, g, s_jobs, wsm, nxt);
