@@ -653,8 +653,10 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
                                  (unsigned long long*)(dbase + off_q[2])};
     if (timing) cudaEventRecord(ctx->ev[1], s);
     if (stime) cudaEventRecord(ctx->split.ev[1], sq);
+    const bool spec = sh.kernel == 2;  // the blocked kernel reads first entries early (kSpecSlots zeroed slots)
+    const int nz = spec ? (int)std::min<unsigned long long>(total_bricks, hdk::kSpecSlots) : 0;
     e = hdk::launch_setup(ddesc, n, setup_tiles, split ? prep_sms : 0, djobs, dstates, dq[g0 % 3], dctl, g0, bxw, by, bz,
-                          setup_mode, sq);
+                          setup_mode, sq, dq[(g0 + 1) % 3], dq[(g0 + 2) % 3], nz);
     if (e == cudaSuccess && split) {
         // the dilation follows the set-up; the caller's stream follows the
         // packing's reads of its masks (work it queues later may overwrite
@@ -688,6 +690,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     sp.stats = stats ? 1 : 0;
     sp.spread = sh.spread;
     sp.job_cache = (n == 1 && sh.kernel == 2) ? hdk::kJobCache : 0;  // a single pair's two jobs
+    sp.spec_first = nz;  // slots of each queue the set-up zeroed
     sp.timeout_ns = ctx->opt.barrier_timeout_ns > 0 ? ctx->opt.barrier_timeout_ns : 10000000000LL;
     const int occ = occupancy_of(ctx, solve_fn, sh.threads, sh.smem);
     if (occ <= 0) return set_error(ctx, HD_ERR_CUDA, "dilation kernel cannot be made resident");

@@ -166,9 +166,12 @@ struct __align__(128) Job {
 };
 static_assert(__builtin_offsetof(Job, U) <= 128, "hot fields of a job within its first line");
 
-// Queue entry: epoch (8 bits) | job (24 bits) | local brick (32 bits).
+// Queue entry: epoch (8 bits) | 1 (bit 55: an entry is never zero, so a
+// cleared slot reads as empty) | job (23 bits) | local brick (32 bits).
+constexpr unsigned kEntryJobMask = 0x7fffffu;
 __host__ __device__ __forceinline__ unsigned long long make_entry(uint32_t epoch, uint32_t job, uint32_t lb) {
-    return ((unsigned long long)(epoch & 0xffu) << 56) | ((unsigned long long)(job & 0xffffffu) << 32) | lb;
+    return ((unsigned long long)(epoch & 0xffu) << 56) | (1ull << 55) |
+           ((unsigned long long)(job & kEntryJobMask) << 32) | lb;
 }
 
 // Mutable per-job state.
@@ -234,7 +237,13 @@ struct SolveParams {
     // job_cache 0: none
     int32_t job_cache;
     int32_t job_cache_base;
+    // blocked kernel: the leading slots of each queue that are zero before a
+    // step's entries are written (the set-up zeroes them; the kernel keeps
+    // them so); a warp numbered below reads its first entry of the next
+    // step before the grid barrier (see solve_tb_kernel); 0: never
+    int32_t spec_first;
 };
+constexpr int kSpecSlots = 4096;  // at least the warps of any persistent grid
 constexpr int kJobCache = 2;
 
 }  // namespace hdk

@@ -17,9 +17,11 @@ namespace hdk {
 // device's); the grid is one resident wave of them.
 cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, int grid, int label, int sms,
                         cudaStream_t s);
+// zq1 / zq2 (may be null): queues whose first nz slots are zeroed.
 cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int sms, Job* jobs,
                          JobState* states, unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
-                         int mode, cudaStream_t s);
+                         int mode, cudaStream_t s, unsigned long long* zq1 = nullptr,
+                         unsigned long long* zq2 = nullptr, int nz = 0);
 // Start values of descs[i].info (counts 0, empty bounding box), i < npairs;
 // with slot_descs, also copies descs[i] to slot_descs[descs[i].job0 / 2].
 cudaError_t launch_info_init(const PairDesc* d_descs, int npairs, cudaStream_t s, PairDesc* slot_descs = nullptr);

@@ -433,10 +433,18 @@ __device__ __forceinline__ long long setup_tile(const PairDesc& P, long long til
 //                         more than the extra bricks)
 __global__ void __launch_bounds__(256) setup_kernel(const PairDesc* __restrict__ descs, int npairs, long long ntiles,
                                                     Job* jobs, JobState* states, unsigned long long* queue0,
-                                                    Ctl* ctl, int g0, int bxw, int by, int bz, int mode) {
+                                                    Ctl* ctl, int g0, int bxw, int by, int bz, int mode,
+                                                    unsigned long long* zq1, unsigned long long* zq2, int nz) {
     __shared__ unsigned s_base;
     int pi = -1;
     const long long G = gridDim.x;
+    // the first nz slots of the two queues the first step does not read
+    // (the dilation kernel reads a warp's next first entry early where a
+    // slot is non-zero)
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nz; t += G * blockDim.x) {
+        zq1[t] = 0ull;
+        zq2[t] = 0ull;
+    }
     // CTAs stride over the tiles: a pair's domain fills only the first of
     // its tiles, so contiguous runs would leave some CTAs without work
     for (long long tile = blockIdx.x; tile < ntiles; tile += G) {
@@ -673,7 +681,7 @@ cudaError_t launch_pack(const PairDesc* d_descs, int npairs, long long ntiles, i
 
 cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, int sms, Job* jobs,
                          JobState* states, unsigned long long* queue0, Ctl* ctl, int g0, int bxw, int by, int bz,
-                         int mode, cudaStream_t s) {
+                         int mode, cudaStream_t s, unsigned long long* zq1, unsigned long long* zq2, int nz) {
     // one wave of resident CTAs (per device, from the occupancy calculator):
     // CTAs whose tiles have nothing to do leave at once, later waves would
     // only add their scheduling
@@ -699,7 +707,7 @@ cudaError_t launch_setup(const PairDesc* d_descs, int npairs, long long ntiles, 
     long long grid = std::min<long long>((long long)per_sm * nsm, ntiles);
     if (grid < 1) grid = 1;
     setup_kernel<<<(unsigned)grid, 256, 0, s>>>(d_descs, npairs, ntiles, jobs, states, queue0, ctl, g0, bxw, by, bz,
-                                                mode);
+                                                mode, zq1, zq2, zq1 && zq2 ? nz : 0);
     return cudaGetLastError();
 }
 

@@ -60,6 +60,11 @@ __device__ __forceinline__ void atom_exch_release_u64(unsigned long long* p, uns
     asm volatile("atom.release.gpu.global.exch.b64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
     (void)old;
 }
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
     unsigned v;
     asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -441,7 +446,7 @@ __global__ void __launch_bounds__(256, 2) solve_kernel(SolveParams p) {
             const unsigned long long* Q = qi == 0 ? p.queue[0] : (qi == 1 ? p.queue[1] : p.queue[2]);
             for (unsigned i = gw; i < cnt; i += nw) {
                 const unsigned long long e = Q[i];
-                brick_step<BXW, BZ, SE18>(p, (int)((e >> 32) & 0xffffffu), (unsigned)e, (unsigned)(e >> 56), g);
+                brick_step<BXW, BZ, SE18>(p, (int)((e >> 32) & kEntryJobMask), (unsigned)e, (unsigned)(e >> 56), g);
             }
             const bool cont = grid_step_barrier(ctl, gen, g, p.timeout_ns, &s_flag, &s_cnt, p.yield, p.yield_gen);
             ++g;

@@ -178,7 +178,7 @@ template <int T>
 __device__ __forceinline__ bool tb_decode(const SolveParams& p, unsigned long long e, int g, const Job* jcache,
                                           TbItem& it) {
     const int lane = threadIdx.x & 31;
-    it.jid = (int)((e >> 32) & 0xffffffu);
+    it.jid = (int)((e >> 32) & kEntryJobMask);
     it.lb = (unsigned)e;
     it.epoch = (unsigned)(e >> 56);
     it.st = p.states + it.jid;
@@ -605,6 +605,7 @@ __global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel
     const unsigned nw = gridDim.x * wpb;
     int g = p.g0;
     int it = 0;
+    unsigned long long e_spec = 0ull;  // this warp's first entry of the step, read before the barrier
     unsigned char* wsm = tb_smem + (threadIdx.x >> 5) * tb_warp_bytes(T, BZ);
     if (cnt > 0) {
         for (;;) {
@@ -634,7 +635,18 @@ __global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel
             // ahead: a claim precedes every dynamic next item, the first one
             // here when the warp's static share is its first item alone
             if (ahead && S < cnt && i < cnt && i + nw >= S && lane0) c_next = atomicAdd(claimp, 1u);
-            if (i < cnt) tb_issue<T, BZ>(p, Q[i], g, s_jobs, wsm, cur);
+            // The warp's first entry: the one read before the barrier if that
+            // slot was already written (a slot below spec_first is zero until
+            // its step's entry is written, so a non-zero value is that
+            // entry), else a load now.  The slot is then cleared, and a slot
+            // of the launch's first queue without an entry is zeroed.
+            unsigned long long e0 = 0ull;
+            if (i < cnt) e0 = e_spec != 0ull ? e_spec : Q[i];
+            if ((int)gw < p.spec_first && (i < cnt || it == 0)) {
+                __syncwarp();  // every lane's read of the slot precedes the clear
+                if (lane0) const_cast<unsigned long long*>(Q)[gw] = 0ull;
+            }
+            if (i < cnt) tb_issue<T, BZ>(p, e0, g, s_jobs, wsm, cur);
             while (i < cnt) {
                 unsigned in = i + nw;
                 const bool late = !ahead && in >= S && S < cnt;  // claimed after this brick
@@ -653,6 +665,13 @@ __global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel
                 if (cur.live) tb_epilogue<T, SE18>(p, cur, res, g);
                 cur = nxt;
                 i = in;
+            }
+            // the first entry of the next step, if its producer has written
+            // it already (the barrier's wait hides the load)
+            {
+                const int qn = (g + 1) % 3;
+                const unsigned long long* Qn = qn == 0 ? p.queue[0] : (qn == 1 ? p.queue[1] : p.queue[2]);
+                e_spec = (int)gw < p.spec_first ? ld_relaxed_u64(Qn + gw) : 0ull;
             }
             const bool cont = grid_step_barrier(ctl, gen, g, p.timeout_ns, &s_flag, &s_cnt, p.yield, p.yield_gen);
             ++g;
