@@ -610,7 +610,7 @@ __global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel
     if (cnt > 0) {
         for (;;) {
             const int qi = g % 3;
-            const unsigned long long* Q = qi == 0 ? p.queue[0] : (qi == 1 ? p.queue[1] : p.queue[2]);
+            unsigned long long* Q = qi == 0 ? p.queue[0] : (qi == 1 ? p.queue[1] : p.queue[2]);
             // Items to warps: a static stride (warp w takes entries w,
             // w + warps, ...) for the first part of the queue, the rest one
             // at a time from a counter, to whichever warp is free first
@@ -644,7 +644,7 @@ __global__ void __launch_bounds__(kTbWarps * 32, tb_min_ctas(T)) solve_tb_kernel
             if (i < cnt) e0 = e_spec != 0ull ? e_spec : Q[i];
             if ((int)gw < p.spec_first && (i < cnt || it == 0)) {
                 __syncwarp();  // every lane's read of the slot precedes the clear
-                if (lane0) const_cast<unsigned long long*>(Q)[gw] = 0ull;
+                if (lane0) Q[gw] = 0ull;
             }
             if (i < cnt) tb_issue<T, BZ>(p, e0, g, s_jobs, wsm, cur);
             while (i < cnt) {
