@@ -134,28 +134,45 @@ __device__ __forceinline__ bool grid_step_barrier(Ctl* ctl, unsigned& gen, int g
 
 // Robust HD on the device, one warp: the stopping rule of hello.cu:1751-1758
 // (keep dilating while (float)total * p > covered, covered = voxels with
-// distance 1..k) on a per-step histogram.  covered grows with k, so the
-// first k that stops is found 32 steps at a time by a prefix sum and a
-// ballot (a single thread would wait on one load per step).
-__device__ __forceinline__ int robust_k_warp(const unsigned long long* hist, int len, unsigned long long total,
-                                             float p) {
+// distance 1..k) on a per-step histogram, for both directions; the result is
+// the later of their stopping steps.  covered grows with k, so the first k
+// that stops is found 32 steps at a time by a prefix sum and a ballot (a
+// single thread would wait on one load per step); the two histograms' words
+// of a round are loaded together, and a direction that has stopped loads
+// nothing more.
+__device__ __forceinline__ int robust_k_warp2(const unsigned long long* ha, unsigned long long ta,
+                                              const unsigned long long* hb, unsigned long long tb, int len,
+                                              float p) {
     const int lane = threadIdx.x & 31;
-    const float tf = (float)total * p;
-    unsigned long long base = 0;
-    for (int k0 = 0; k0 < len; k0 += 32) {
+    const float tfa = (float)ta * p, tfb = (float)tb * p;
+    unsigned long long base_a = 0, base_b = 0;
+    int ka = -1, kb = -1;
+    for (int k0 = 0; k0 < len && (ka < 0 || kb < 0); k0 += 32) {
         const int k = k0 + lane;
-        unsigned long long c = (k > 0 && k < len) ? hist[k] : 0ull;
+        const bool in = k > 0 && k < len;
+        unsigned long long ca = (ka < 0 && in) ? ha[k] : 0ull;
+        unsigned long long cb = (kb < 0 && in) ? hb[k] : 0ull;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const unsigned long long t = __shfl_up_sync(kFull, c, o);
-            if (lane >= o) c += t;
+            const unsigned long long xa = __shfl_up_sync(kFull, ca, o);
+            const unsigned long long xb = __shfl_up_sync(kFull, cb, o);
+            if (lane >= o) {
+                ca += xa;
+                cb += xb;
+            }
         }
-        const bool stop = k < len && !(tf > (float)(base + c));
-        const unsigned m = __ballot_sync(kFull, stop);
-        if (m) return k0 + __ffs(m) - 1;
-        base += __shfl_sync(kFull, c, 31);
+        if (ka < 0) {
+            const unsigned m = __ballot_sync(kFull, k < len && !(tfa > (float)(base_a + ca)));
+            if (m) ka = k0 + __ffs(m) - 1;
+            base_a += __shfl_sync(kFull, ca, 31);
+        }
+        if (kb < 0) {
+            const unsigned m = __ballot_sync(kFull, k < len && !(tfb > (float)(base_b + cb)));
+            if (m) kb = k0 + __ffs(m) - 1;
+            base_b += __shfl_sync(kFull, cb, 31);
+        }
     }
-    return len - 1;
+    return max(ka < 0 ? len - 1 : ka, kb < 0 ? len - 1 : kb);
 }
 
 // Decodes pair i's result on the device (one warp), with the rules of the
@@ -195,8 +212,7 @@ static __device__ __noinline__ void decode_pair_warp(const SolveParams& p, int i
         r.hd = max(r.hd_ab, r.hd_ba);
         r.avg_hd = (double)(r.sum_ab + r.sum_ba) / (double)(r.n_a + r.n_b);
         const int kp1 = P.kmax + 1;
-        r.hd_robust = max(robust_k_warp(P.hist[1], kp1, r.n_a_not_b, p.pct),
-                          robust_k_warp(P.hist[0], kp1, r.n_b_not_a, p.pct));
+        r.hd_robust = robust_k_warp2(P.hist[1], r.n_a_not_b, P.hist[0], r.n_b_not_a, kp1, p.pct);
         if (st != HD_OK) r.hd = r.hd_ab = r.hd_ba = r.hd_robust = -1;
     }
     if ((threadIdx.x & 31) == 0) p.out[i] = r;
