@@ -275,9 +275,10 @@ def bench_ours(args):
 
     # ---- phases of the launches the value path times --------------------------
     # the pipelined entry packs on a few SMs and dilates on the rest: CUDA
-    # events on those streams around each kernel (the last of a few
-    # back-to-back calls, whose dilation has no packing beside it; over the
-    # four sequences the last pair alternates between the two pairs)
+    # events on those streams around each kernel (the last of three
+    # back-to-back calls: no packing runs beside its dilation, the previous
+    # pair's dilation may, on the other SM group; over the four sequences the
+    # last pair alternates between the two pairs)
     split_ph = []
     for k in range(4):
         for j in range(3):
@@ -335,6 +336,16 @@ def bench_ours(args):
             "setup_ms": round(statistics.mean(p["setup_ms"] for p in split_ph), 4),
             "achieved": round(b_iter / (so_split * 1e-3) / 1e9, 1)}
         value_launch["frac"] = round(value_launch["achieved"] / peak, 4)
+        parts = split_ph[0].get("dilation_partitions", 1)
+        value_launch["dilation_partitions"] = parts
+        if parts == 2:
+            # consecutive pairs dilate side by side on two SM groups: per
+            # launch the time is longer, per pair the pipeline moves the
+            # frontier bytes at the value leg's rate
+            value_launch["launch"] += ", two such launches in flight on disjoint SM groups"
+            value_launch["pipeline"] = {
+                "what": "frontier bytes of the value leg's pairs per second of its timed region",
+                "achieved": round(b_iter * value / 1e9, 1), "frac": round(b_iter * value / 1e9 / peak, 4)}
         achieved = value_launch["achieved"]
         so = so_split
     roofline = {
@@ -384,8 +395,9 @@ def bench_ours(args):
                 "blocking_path": "hd_compute_u8, one call per pair, masks read in place over the host link",
                 "staged_copy_ms_per_step": round(staged_ms, 4)},
         "gpu_launches": 3 * args.steps,  # per pair: pack, set-up, persistent dilation (decodes the result too)
-        "value_path": "hd_compute_u8_device_pipelined x K, hd_pipeline_flush: pair k+1's packing and set-up on "
-                      "a few SMs beside pair k's dilation on the rest (green contexts)",
+        "value_path": "hd_compute_u8_device_pipelined x K, hd_pipeline_flush: packing and set-up on 40 SMs, "
+                      "consecutive pairs dilating side by side on two groups of 56 (green contexts, four "
+                      "workspaces in turn)",
         "async_serial": {"path": "hd_compute_u8_device_async x K (each pair after the previous one)",
                          "ms_per_step": round(serial_ms, 4), "pairs_per_s": round(1000.0 / serial_ms, 1)},
         "blocking_call": {"path": "hd_compute_u8_device (returns the result to the host each call)",

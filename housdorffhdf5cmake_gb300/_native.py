@@ -91,6 +91,7 @@ class HdTimings(ctypes.Structure):
         ("kernel", ctypes.c_int32),
         ("steps_per_barrier", ctypes.c_int32),
         ("brick_rows", ctypes.c_int32),
+        ("dilation_partitions", ctypes.c_int32),
     ]
 
     def as_dict(self) -> dict:

@@ -190,20 +190,32 @@ using GreenDestroyFn = CUresult (*)(CUgreenCtx);
 
 }  // namespace
 
-// SMs given to packing and set-up on the split path (a multiple of the
-// partition granularity, 8 SMs on GB300); the rest dilate.  Measured on the
-// 512x512x256 pairs: 24 / 32 / 48 / 64 SMs -> 155 / 127 / 112 / 121 us per
-// pair (142 us unsplit).
-constexpr unsigned kSplitPrepSms = 48;
+// The split path's SM partitions (green contexts; the granularity is 8 SMs
+// on GB300).  One dilation partition: packing and set-up on 48 SMs, each
+// pair's dilation on the other 104 in turn.  Two: packing and set-up on 40,
+// the rest in two groups of 56, consecutive pairs dilating side by side
+// (workspace i on group i % 2, four workspaces in turn).  Measured on the
+// two 512x512x256 pairs alternating (0.142 ms per pair unsplit): one
+// partition with 24 / 32 / 48 / 64 packing SMs 0.155 / 0.127 / 0.107 / 0.121
+// ms per pair; two partitions with 40 / 56 packing SMs (groups of 56 / 48)
+// 0.094 / 0.102 ms, with two workspaces instead of four 0.137 ms (a
+// packing waited for the dilation before last in its partition).  A lone
+// pair's latency is higher on 56 dilation SMs (0.30 against 0.23 ms).
+constexpr int kSplitDilations = 2;
+constexpr unsigned kSplitPrepSms[2] = {48, 40};  // by dilation partitions
 
-// HD_SPLIT_SMS in the environment overrides it: 0 = no split (profilers
-// that cannot follow kernels into green contexts), else the SMs to give to
-// packing and set-up.
+// HD_SPLIT_DILATIONS (1 or 2) in the environment overrides the dilation
+// partitions, HD_SPLIT_SMS the packing SMs: 0 = no split (profilers that
+// cannot follow kernels into green contexts), else the SMs to give to
+// packing and set-up (two partitions: the rest in two equal groups, rounded
+// up to the granularity).
 bool split_ready(hd_context* ctx) {
     hd_context::Split& sp = ctx->split;
     if (sp.state) return sp.state > 0;
     sp.state = -1;
-    unsigned prep_want = kSplitPrepSms;
+    int parts = kSplitDilations;
+    if (const char* env = std::getenv("HD_SPLIT_DILATIONS")) parts = std::strtol(env, nullptr, 10) == 1 ? 1 : 2;
+    unsigned prep_want = kSplitPrepSms[parts - 1];
     if (const char* env = std::getenv("HD_SPLIT_SMS")) {
         const long v = std::strtol(env, nullptr, 10);
         if (v <= 0) return false;
@@ -219,27 +231,51 @@ bool split_ready(hd_context* ctx) {
     auto stream = driver_fn<CUresult (*)(CUstream*, CUgreenCtx, unsigned, int)>("cuGreenCtxStreamCreate", 12050);
     if (!get_dev || !get_res || !split || !make_desc || !create || !stream) return false;
     CUdevice dev;
-    CUdevResource all{}, prep{}, rest{};
-    unsigned groups = 1;
+    CUdevResource all{};
     if (get_dev(&dev, ctx->device) != CUDA_SUCCESS || get_res(dev, &all, CU_DEV_RESOURCE_TYPE_SM) != CUDA_SUCCESS)
         return false;
     if (all.sm.smCount < prep_want + 64) return false;  // too few SMs to give some away
-    if (split(&prep, &groups, &all, &rest, 0, prep_want) != CUDA_SUCCESS || groups != 1) return false;
-    CUdevResourceDesc d[2];
-    CUgreenCtx g[2] = {nullptr, nullptr};
-    CUstream st[2] = {nullptr, nullptr};
-    bool ok = make_desc(&d[0], &rest, 1) == CUDA_SUCCESS && make_desc(&d[1], &prep, 1) == CUDA_SUCCESS;
-    for (int i = 0; i < 2 && ok; ++i) ok = create(&g[i], d[i], dev, CU_GREEN_CTX_DEFAULT_STREAM) == CUDA_SUCCESS;
-    for (int i = 0; i < 2 && ok; ++i) ok = stream(&st[i], g[i], CU_STREAM_NON_BLOCKING, 0) == CUDA_SUCCESS;
+    // d[0]: dilations (workspace 0, or both), d[1]: packing and set-up,
+    // d[2]: dilations in workspace 1
+    CUdevResourceDesc d[3];
+    unsigned sms[2] = {0, 0}, prep_sms = 0;
+    bool ok;
+    if (parts == 2) {
+        // two equal dilation groups split off the whole device (a split's
+        // remainder cannot be split again; the group size rounds up to the
+        // partition granularity), the remainder packing
+        CUdevResource half[2]{}, left{};
+        unsigned n2 = 2;
+        ok = split(half, &n2, &all, &left, 0, (all.sm.smCount - prep_want) / 2) == CUDA_SUCCESS && n2 == 2 &&
+             left.sm.smCount >= 8;
+        ok = ok && make_desc(&d[0], &half[0], 1) == CUDA_SUCCESS && make_desc(&d[2], &half[1], 1) == CUDA_SUCCESS &&
+             make_desc(&d[1], &left, 1) == CUDA_SUCCESS;
+        sms[0] = half[0].sm.smCount;
+        sms[1] = half[1].sm.smCount;
+        prep_sms = left.sm.smCount;
+    } else {
+        CUdevResource prep{}, rest{};
+        unsigned groups = 1;
+        ok = split(&prep, &groups, &all, &rest, 0, prep_want) == CUDA_SUCCESS && groups == 1;
+        ok = ok && make_desc(&d[0], &rest, 1) == CUDA_SUCCESS && make_desc(&d[1], &prep, 1) == CUDA_SUCCESS;
+        sms[0] = sms[1] = rest.sm.smCount;
+        prep_sms = prep.sm.smCount;
+    }
+    const int ng = parts == 2 ? 3 : 2;
+    CUgreenCtx g[3] = {nullptr, nullptr, nullptr};
+    CUstream st[3] = {nullptr, nullptr, nullptr};
+    for (int i = 0; i < ng && ok; ++i) ok = create(&g[i], d[i], dev, CU_GREEN_CTX_DEFAULT_STREAM) == CUDA_SUCCESS;
+    for (int i = 0; i < ng && ok; ++i) ok = stream(&st[i], g[i], CU_STREAM_NON_BLOCKING, 0) == CUDA_SUCCESS;
     cudaError_t e = ok ? cudaSuccess : cudaErrorUnknown;
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sp.caller, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sp.prep_done, cudaEventDisableTiming);
-    for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&sp.ws_free[i], cudaEventDisableTiming);
+    for (int i = 0; i < hd_context::Split::kWorkspaces && e == cudaSuccess; ++i)
+        e = cudaEventCreateWithFlags(&sp.ws_free[i], cudaEventDisableTiming);
     if (ctx->opt.record_timings)
         for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&sp.ev[i]);
-    sp.green[0] = g[0];
-    sp.green[1] = g[1];
-    sp.solve = (cudaStream_t)st[0];
+    for (int i = 0; i < 3; ++i) sp.green[i] = g[i];
+    sp.solve[0] = (cudaStream_t)st[0];
+    sp.solve[1] = (cudaStream_t)(ng == 3 ? st[2] : st[0]);
     sp.prep = (cudaStream_t)st[1];
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -247,26 +283,38 @@ bool split_ready(hd_context* ctx) {
         sp.state = -1;
         return false;
     }
-    sp.solve_sms = (int)rest.sm.smCount;
-    sp.prep_sms = (int)prep.sm.smCount;
+    sp.solve_sms[0] = (int)sms[0];
+    sp.solve_sms[1] = (int)sms[1];
+    sp.prep_sms = (int)prep_sms;
+    sp.nws = parts == 2 ? hd_context::Split::kWorkspaces : 2;
     sp.state = 1;
     return true;
 }
 
 void split_release(hd_context* ctx) {
     hd_context::Split& sp = ctx->split;
-    for (cudaStream_t s : {sp.solve, sp.prep})
+    for (cudaStream_t s : {sp.solve[0], sp.solve[1] != sp.solve[0] ? sp.solve[1] : nullptr, sp.prep})
         if (s) {
             cudaStreamSynchronize(s);
             cudaStreamDestroy(s);
         }
-    for (cudaEvent_t ev : {sp.caller, sp.prep_done, sp.ws_free[0], sp.ws_free[1], sp.ev[0], sp.ev[1], sp.ev[2],
-                           sp.ev[3], sp.ev[4]})
+    for (cudaEvent_t ev : {sp.caller, sp.prep_done, sp.ev[0], sp.ev[1], sp.ev[2], sp.ev[3], sp.ev[4]})
+        if (ev) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : sp.ws_free)
         if (ev) cudaEventDestroy(ev);
     auto destroy = driver_fn<GreenDestroyFn>("cuGreenCtxDestroy", 12040);
     for (void* g : sp.green)
         if (g && destroy) destroy((CUgreenCtx)g);
     sp = hd_context::Split{};
+}
+
+// Makes `st` wait for the latest dilation in every workspace of the split
+// path (an event never recorded is no wait).
+cudaError_t wait_split_dilations(hd_context* ctx, cudaStream_t st) {
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < hd_context::Split::kWorkspaces && e == cudaSuccess; ++i)
+        if (ctx->split.ws_free[i]) e = cudaStreamWaitEvent(st, ctx->split.ws_free[i], 0);
+    return e;
 }
 
 namespace {
@@ -463,21 +511,23 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     const bool split = async && ro.pipelined && n == 1 && sh.kernel == 2 &&
                        (double)pairs[0].W * pairs[0].H * pairs[0].D <= (double)(1 << 26) && split_ready(ctx);
     if (!split && ctx->split.pending) {  // every other call follows the pipelined ones
-        cudaError_t e0 = cudaStreamWaitEvent(s, ctx->split.ws_free[ctx->split.last], 0);
+        const cudaError_t e0 = wait_split_dilations(ctx, s);
         if (e0 != cudaSuccess) return cuda_fail(ctx, e0, "pipeline flush");
         ctx->split.pending = false;
     }
     // the workspace alternates only once a dilation has been launched in it
     const int ws = split ? ctx->split.next : 0;
-    DeviceArena& arena = ws ? ctx->arena2 : ctx->arena;
-    cudaStream_t sq = split ? ctx->split.prep : s, sv = split ? ctx->split.solve : s;
+    const int part = ws % 2;  // the split path's dilation partition
+    DeviceArena& arena = ws ? ctx->ws_arena[ws - 1] : ctx->arena;
+    cudaStream_t sq = split ? ctx->split.prep : s, sv = split ? ctx->split.solve[part] : s;
     const int prep_sms = split ? ctx->split.prep_sms : ctx->sm_count;
     // Growing a buffer frees the old one after cudaDeviceSynchronize, which
     // waits for the primary context's streams only: the split path's streams
     // belong to green contexts and may still use it, so drain them first.
     auto drain_split = [&]() {
         if (ctx->split.state > 0) {
-            cudaStreamSynchronize(ctx->split.solve);
+            cudaStreamSynchronize(ctx->split.solve[0]);
+            cudaStreamSynchronize(ctx->split.solve[1]);
             cudaStreamSynchronize(ctx->split.prep);
         }
     };
@@ -495,15 +545,19 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     }
     if (total_bricks > ctx->stamp_slots || ctx->g_next > (1 << 30)) {
         const size_t want = std::max<size_t>(total_bricks, ctx->stamp_slots);
-        if (sizeof(int32_t) * want > ctx->stamps.cap) drain_split();
+        if (sizeof(int32_t) * want > std::min(ctx->stamps.cap, ctx->stamps2.cap)) drain_split();
         e = ctx->stamps.ensure(sizeof(int32_t) * want);
+        if (e == cudaSuccess) e = ctx->stamps2.ensure(sizeof(int32_t) * want);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "brick stamps");
-        // the stamps belong to every dilation of the context: the reset
-        // follows the latest one (split path: a dilation the caller's stream
-        // has not waited for yet; the others precede the caller event that
-        // sq waits for) and precedes this call's
-        if (split && ctx->split.pending) e = cudaStreamWaitEvent(sq, ctx->split.ws_free[ctx->split.last], 0);
+        // the reset follows every dilation that used the stamps (split
+        // path: the latest one in each workspace, which the caller's stream
+        // may not have waited for yet; the others precede the caller event
+        // that sq waits for) and precedes this call's
+        if (split && ctx->split.pending) {
+            e = wait_split_dilations(ctx, sq);
+        }
         if (e == cudaSuccess) e = cudaMemsetAsync(ctx->stamps.ptr, 0, sizeof(int32_t) * want, sq);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->stamps2.ptr, 0, sizeof(int32_t) * want, sq);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "stamp reset");
         ctx->stamp_slots = want;
         ctx->g_next = 1;
@@ -678,7 +732,9 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     sp.jobs = djobs;
     sp.states = dstates;
     for (int q = 0; q < 3; ++q) sp.queue[q] = dq[q];
-    sp.stamps = (int32_t*)ctx->stamps.ptr;
+    // the split path's second dilation partition has its own stamps (its
+    // dilations may run beside those of the first)
+    sp.stamps = (int32_t*)(split && part == 1 ? ctx->stamps2.ptr : ctx->stamps.ptr);
     sp.ctl = dctl;
     sp.map[0] = ro.map_b;  // job 0 covers B
     sp.map[1] = ro.map_a;  // job 1 covers A
@@ -695,7 +751,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     const int occ = occupancy_of(ctx, solve_fn, sh.threads, sh.smem);
     if (occ <= 0) return set_error(ctx, HD_ERR_CUDA, "dilation kernel cannot be made resident");
     const int per_sm = cps > 0 ? std::min(cps, occ) : occ;
-    dim3 grid((split ? ctx->split.solve_sms : ctx->sm_count) * per_sm), block(sh.threads);
+    dim3 grid((split ? ctx->split.solve_sms[part] : ctx->sm_count) * per_sm), block(sh.threads);
     const float pct = (ctx->opt.percentile > 0.f && ctx->opt.percentile <= 1.f) ? ctx->opt.percentile : 0.95f;
     // the launch decodes the results on the device (one warp per pair, after
     // its last barrier): the per-step histograms never leave the device
@@ -717,12 +773,12 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         T.kernel = sh.kernel;
         T.steps_per_barrier = sh.steps;
         T.brick_rows = by;
+        T.dilation_partitions = ctx->split.solve[1] != ctx->split.solve[0] ? 2 : 1;
     }
     if (e == cudaSuccess && split) {
         e = cudaEventRecord(ctx->split.ws_free[ws], sv);
         ctx->split.pending = true;
-        ctx->split.last = ws;
-        ctx->split.next = ws ^ 1;
+        ctx->split.next = (ws + 1) % ctx->split.nws;
     }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "dilation launch");
     if (timing) cudaEventRecord(ctx->ev[3], s);
@@ -769,6 +825,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         T.kernel = sh.kernel;
         T.steps_per_barrier = sh.steps;
         T.brick_rows = by;
+        T.dilation_partitions = 0;
     }
     if (stats && n == 1) {
         const int kp1 = plan[0].kmax + 1;
@@ -894,8 +951,9 @@ hd_status hd_context_destroy(hd_context* ctx) {
         if (ctx->stream) cudaStreamSynchronize(ctx->stream);
         split_release(ctx);
         ctx->arena.release();
-        ctx->arena2.release();
+        for (DeviceArena& a : ctx->ws_arena) a.release();
         ctx->stamps.release();
+        ctx->stamps2.release();
         ctx->pinned.release();
         for (int i = 0; i < hd_context::kAsyncSlots; ++i) {
             ctx->async_stage[i].release();
@@ -1030,9 +1088,10 @@ hd_status hd_pipeline_flush(hd_context* ctx, void* stream) {
     if (!ctx->split.pending) return HD_OK;
     DeviceGuard g(ctx->device);
     if (!g.ok) return set_error(ctx, HD_ERR_CUDA, "cannot select device %d", ctx->device);
-    // the dilations run in order on one stream: the latest covers them all
-    cudaError_t e = cudaStreamWaitEvent(stream ? (cudaStream_t)stream : ctx->stream,
-                                        ctx->split.ws_free[ctx->split.last], 0);
+    // the dilations in each workspace run in order on one stream: the
+    // latest of each covers them all
+    const cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    const cudaError_t e = wait_split_dilations(ctx, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "pipeline flush");
     ctx->split.pending = false;
     return HD_OK;

@@ -101,6 +101,9 @@ struct hd_context {
     int g_next = 1;  // global iteration counter, monotonic across calls (brick stamps rely on it)
     hdh::DeviceArena arena;   // per-call buffers
     hdh::DeviceArena stamps;  // per-brick queue stamps, never cleared
+    // the split path's second workspace's stamps: its dilations may run
+    // beside those in the first workspace (same size and resets as stamps)
+    hdh::DeviceArena stamps2;
     size_t stamp_slots = 0;
     hdh::PinnedArena pinned;
     std::map<const void*, int> occupancy;  // persistent kernel -> resident CTAs per SM
@@ -125,14 +128,22 @@ struct hd_context {
     // the two alternate between two workspaces
     struct Split {
         int state = 0;                      // 0 not tried, 1 ready, -1 unavailable
-        void* green[2] = {nullptr, nullptr};  // CUgreenCtx: [0] dilation, [1] packing and set-up
-        cudaStream_t solve = nullptr, prep = nullptr;
-        int solve_sms = 0, prep_sms = 0;
+        // CUgreenCtx: [0] dilations in workspace 0, [1] packing and set-up,
+        // [2] dilations in workspace 1 (two dilation partitions only)
+        void* green[3] = {nullptr, nullptr, nullptr};
+        // solve[p]: the dilations of partition p (one stream for both with
+        // one dilation partition); workspace i dilates on partition i % 2
+        cudaStream_t solve[2] = {nullptr, nullptr}, prep = nullptr;
+        int solve_sms[2] = {0, 0}, prep_sms = 0;
         cudaEvent_t caller = nullptr, prep_done = nullptr;
-        cudaEvent_t ws_free[2] = {nullptr, nullptr};  // the dilation that last used workspace i
+        // workspaces in turn: 2 with one dilation partition, 4 with two (a
+        // pair's packing then need not wait for the dilation before last in
+        // its partition)
+        static constexpr int kWorkspaces = 4;
+        int nws = 2;
+        cudaEvent_t ws_free[kWorkspaces] = {};  // the dilation that last used workspace i
         int next = 0;
         bool pending = false;  // a dilation the caller's stream has not waited for yet
-        int last = 0;          // the workspace of the latest dilation
         // record_timings: events of the latest call on the split SMs, each on
         // the stream its kernel ran on (before pack, after pack, after
         // set-up; before and after the dilation); read by
@@ -141,7 +152,7 @@ struct hd_context {
         bool timed = false;
         hd_timings shape{};  // the fields of hd_timings that are not times
     } split;
-    hdh::DeviceArena arena2;  // the split path's second workspace
+    hdh::DeviceArena ws_arena[Split::kWorkspaces - 1];  // the split path's workspaces 1, 2, ...
 };
 
 namespace hdh {

@@ -115,6 +115,9 @@ typedef struct hd_timings {
     int32_t kernel;      /* 1 = one step per barrier, 2 = temporally blocked */
     int32_t steps_per_barrier;
     int32_t brick_rows;
+    int32_t dilation_partitions; /* pipelined entry on split SMs: dilations in
+                                    flight side by side on disjoint SM groups
+                                    (1 or 2); 0 on the other entries */
 } hd_timings;
 
 typedef struct hd_context hd_context;

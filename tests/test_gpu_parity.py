@@ -370,13 +370,16 @@ def test_async_entry_matches_blocking_entry(hd, ctx):
                                         None) == hd.HD_ERR_BAD_ARG
 
 
-def test_pipelined_entry_matches_blocking_entry(hd, ctx):
-    """hd_compute_u8_device_pipelined: back-to-back pairs (two workspaces in
-    turn on split SMs; the 512x512x257 pair is above the split's size limit
-    and runs like the asynchronous entry), a blocking call in the middle
-    (which waits for the pipelined ones first), results complete after
-    flush(), equal field by field to hd_compute_u8_device."""
+@pytest.mark.parametrize("partitions", [1, 2])
+def test_pipelined_entry_matches_blocking_entry(hd, ctx, partitions, monkeypatch):
+    """hd_compute_u8_device_pipelined: back-to-back pairs (on split SMs: one
+    dilation partition with two workspaces in turn, or two side by side with
+    four; the 512x512x257 pair is above the split's size limit and runs like
+    the asynchronous entry), a blocking call in the middle (which waits for
+    the pipelined ones first), results complete after flush(), equal field by
+    field to hd_compute_u8_device."""
     from housdorffhdf5cmake_gb300 import _native as N
+    monkeypatch.setenv("HD_SPLIT_DILATIONS", str(partitions))  # read when the context first splits
     rng = np.random.default_rng(8)
     cases = []
     for i, shape in enumerate([(24, 40, 56), (64, 96, 130), (9, 17, 33), (80, 120, 200)]):
@@ -388,7 +391,7 @@ def test_pipelined_entry_matches_blocking_entry(hd, ctx):
     z = torch.zeros((12, 20, 36), dtype=torch.uint8, device="cuda")
     cases.append((z, z.clone(), "se6"))
     want = [ctx.compute(a, b, m) for a, b, m in cases]
-    with hd.Context(0) as c:
+    with hd.Context(0, record_timings=True) as c:
         outs = []
         for rep in range(2):
             for i, (a, b, m) in enumerate(cases):
@@ -398,6 +401,8 @@ def test_pipelined_entry_matches_blocking_entry(hd, ctx):
         c.flush()
         torch.cuda.current_stream().synchronize()
         got = [hd.result_from_bytes(o.cpu()) for o in outs]
+        tm = c.last_timings()  # the last pair ran on split SMs
+        assert tm["iterations"] == -1 and tm["dilation_partitions"] == partitions, tm
     for k in want[0]:
         assert mid[k] == want[0][k] or (k == "avg_hd" and mid[k] != mid[k])
     for i, g in enumerate(got):
