@@ -338,11 +338,11 @@ def bench_ours(args):
         value_launch["frac"] = round(value_launch["achieved"] / peak, 4)
         parts = split_ph[0].get("dilation_partitions", 1)
         value_launch["dilation_partitions"] = parts
-        if parts == 2:
-            # consecutive pairs dilate side by side on two SM groups: per
+        if parts > 1:
+            # consecutive pairs dilate side by side on several SM groups: per
             # launch the time is longer, per pair the pipeline moves the
             # frontier bytes at the value leg's rate
-            value_launch["launch"] += ", two such launches in flight on disjoint SM groups"
+            value_launch["launch"] += f", {parts} such launches in flight on disjoint SM groups"
             value_launch["pipeline"] = {
                 "what": "frontier bytes of the value leg's pairs per second of its timed region",
                 "achieved": round(b_iter * value / 1e9, 1), "frac": round(b_iter * value / 1e9 / peak, 4)}
@@ -395,8 +395,8 @@ def bench_ours(args):
                 "blocking_path": "hd_compute_u8, one call per pair, masks read in place over the host link",
                 "staged_copy_ms_per_step": round(staged_ms, 4)},
         "gpu_launches": 3 * args.steps,  # per pair: pack, set-up, persistent dilation (decodes the result too)
-        "value_path": "hd_compute_u8_device_pipelined x K, hd_pipeline_flush: packing and set-up on 40 SMs, "
-                      "consecutive pairs dilating side by side on two groups of 56 (green contexts, four "
+        "value_path": "hd_compute_u8_device_pipelined x K, hd_pipeline_flush: packing and set-up on 56 SMs, "
+                      "consecutive pairs dilating side by side on three groups of 32 (green contexts, six "
                       "workspaces in turn)",
         "async_serial": {"path": "hd_compute_u8_device_async x K (each pair after the previous one)",
                          "ms_per_step": round(serial_ms, 4), "pairs_per_s": round(1000.0 / serial_ms, 1)},

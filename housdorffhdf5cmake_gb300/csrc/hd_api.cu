@@ -192,29 +192,38 @@ using GreenDestroyFn = CUresult (*)(CUgreenCtx);
 
 // The split path's SM partitions (green contexts; the granularity is 8 SMs
 // on GB300).  One dilation partition: packing and set-up on 48 SMs, each
-// pair's dilation on the other 104 in turn.  Two: packing and set-up on 40,
-// the rest in two groups of 56, consecutive pairs dilating side by side
-// (workspace i on group i % 2, four workspaces in turn).  Measured on the
-// two 512x512x256 pairs alternating (0.142 ms per pair unsplit): one
-// partition with 24 / 32 / 48 / 64 packing SMs 0.155 / 0.127 / 0.107 / 0.121
-// ms per pair; two partitions with 40 / 56 packing SMs (groups of 56 / 48)
-// 0.094 / 0.102 ms, with two workspaces instead of four 0.137 ms (a
-// packing waited for the dilation before last in its partition).  A lone
-// pair's latency is higher on 56 dilation SMs (0.30 against 0.23 ms).
-constexpr int kSplitDilations = 2;
-constexpr unsigned kSplitPrepSms[2] = {48, 40};  // by dilation partitions
+// pair's dilation on the other 104 in turn.  Two or three: packing and
+// set-up on 40 / 56 SMs, the rest in equal groups (56 / 32 SMs),
+// consecutive pairs dilating side by side (workspace i on group i % parts,
+// two workspaces per group in turn).  A single pair's dilation is
+// latency-bound: on fewer SMs it takes longer, but much less than in
+// proportion (the 512x512x256 pairs: 0.124 / 0.077 ms on 104 SMs, 0.178 /
+// 0.077 ms on 56, 0.179 ms on average over both on 32), so side by side the groups
+// finish more pairs per second.  Measured on those two pairs alternating
+// (0.142 ms per pair unsplit): one partition with 24 / 32 / 48 / 64
+// packing SMs 0.155 / 0.127 / 0.107 / 0.121 ms per pair; two partitions
+// with 40 / 56 packing SMs (groups of 56 / 48) 0.094 / 0.102 ms, with one
+// workspace per group 0.137 ms (a packing waited for the dilation before
+// last in its group); three with 56 / 32 packing SMs (groups of 32 / 40)
+// 0.080 / 0.115 ms: packing and set-up on 56 SMs (0.073 ms a pair) set the
+// pace.  A lone pair's latency is higher on fewer dilation SMs (0.30 ms
+// on 56 against 0.23 ms on 104).
+constexpr int kSplitDilations = 3;
+constexpr unsigned kSplitPrepSms[hd_context::kMaxDilationParts] = {48, 40, 56};  // by dilation partitions
 
-// HD_SPLIT_DILATIONS (1 or 2) in the environment overrides the dilation
+// HD_SPLIT_DILATIONS (1 to 3) in the environment overrides the dilation
 // partitions, HD_SPLIT_SMS the packing SMs: 0 = no split (profilers that
 // cannot follow kernels into green contexts), else the SMs to give to
-// packing and set-up (two partitions: the rest in two equal groups, rounded
+// packing and set-up (several partitions: the rest in equal groups, rounded
 // up to the granularity).
 bool split_ready(hd_context* ctx) {
+    constexpr int kMax = hd_context::kMaxDilationParts;
     hd_context::Split& sp = ctx->split;
     if (sp.state) return sp.state > 0;
     sp.state = -1;
     int parts = kSplitDilations;
-    if (const char* env = std::getenv("HD_SPLIT_DILATIONS")) parts = std::strtol(env, nullptr, 10) == 1 ? 1 : 2;
+    if (const char* env = std::getenv("HD_SPLIT_DILATIONS"))
+        parts = (int)std::min<long>(std::max<long>(std::strtol(env, nullptr, 10), 1), kMax);
     unsigned prep_want = kSplitPrepSms[parts - 1];
     if (const char* env = std::getenv("HD_SPLIT_SMS")) {
         const long v = std::strtol(env, nullptr, 10);
@@ -235,35 +244,35 @@ bool split_ready(hd_context* ctx) {
     if (get_dev(&dev, ctx->device) != CUDA_SUCCESS || get_res(dev, &all, CU_DEV_RESOURCE_TYPE_SM) != CUDA_SUCCESS)
         return false;
     if (all.sm.smCount < prep_want + 64) return false;  // too few SMs to give some away
-    // d[0]: dilations (workspace 0, or both), d[1]: packing and set-up,
-    // d[2]: dilations in workspace 1
-    CUdevResourceDesc d[3];
-    unsigned sms[2] = {0, 0}, prep_sms = 0;
+    // d[0]: packing and set-up, d[1 + p]: dilation partition p
+    CUdevResourceDesc d[1 + kMax];
+    unsigned sms[kMax] = {}, prep_sms = 0;
     bool ok;
-    if (parts == 2) {
-        // two equal dilation groups split off the whole device (a split's
+    if (parts > 1) {
+        // equal dilation groups split off the whole device (a split's
         // remainder cannot be split again; the group size rounds up to the
-        // partition granularity), the remainder packing
-        CUdevResource half[2]{}, left{};
-        unsigned n2 = 2;
-        ok = split(half, &n2, &all, &left, 0, (all.sm.smCount - prep_want) / 2) == CUDA_SUCCESS && n2 == 2 &&
-             left.sm.smCount >= 8;
-        ok = ok && make_desc(&d[0], &half[0], 1) == CUDA_SUCCESS && make_desc(&d[2], &half[1], 1) == CUDA_SUCCESS &&
-             make_desc(&d[1], &left, 1) == CUDA_SUCCESS;
-        sms[0] = half[0].sm.smCount;
-        sms[1] = half[1].sm.smCount;
+        // granularity), the remainder packing
+        CUdevResource grp[kMax]{}, left{};
+        unsigned n = (unsigned)parts;
+        ok = split(grp, &n, &all, &left, 0, (all.sm.smCount - prep_want) / parts) == CUDA_SUCCESS &&
+             n == (unsigned)parts && left.sm.smCount >= 8;
+        ok = ok && make_desc(&d[0], &left, 1) == CUDA_SUCCESS;
+        for (int q = 0; q < parts && ok; ++q) {
+            ok = make_desc(&d[1 + q], &grp[q], 1) == CUDA_SUCCESS;
+            sms[q] = grp[q].sm.smCount;
+        }
         prep_sms = left.sm.smCount;
     } else {
         CUdevResource prep{}, rest{};
         unsigned groups = 1;
         ok = split(&prep, &groups, &all, &rest, 0, prep_want) == CUDA_SUCCESS && groups == 1;
-        ok = ok && make_desc(&d[0], &rest, 1) == CUDA_SUCCESS && make_desc(&d[1], &prep, 1) == CUDA_SUCCESS;
-        sms[0] = sms[1] = rest.sm.smCount;
+        ok = ok && make_desc(&d[0], &prep, 1) == CUDA_SUCCESS && make_desc(&d[1], &rest, 1) == CUDA_SUCCESS;
+        sms[0] = rest.sm.smCount;
         prep_sms = prep.sm.smCount;
     }
-    const int ng = parts == 2 ? 3 : 2;
-    CUgreenCtx g[3] = {nullptr, nullptr, nullptr};
-    CUstream st[3] = {nullptr, nullptr, nullptr};
+    const int ng = 1 + parts;
+    CUgreenCtx g[1 + kMax] = {};
+    CUstream st[1 + kMax] = {};
     for (int i = 0; i < ng && ok; ++i) ok = create(&g[i], d[i], dev, CU_GREEN_CTX_DEFAULT_STREAM) == CUDA_SUCCESS;
     for (int i = 0; i < ng && ok; ++i) ok = stream(&st[i], g[i], CU_STREAM_NON_BLOCKING, 0) == CUDA_SUCCESS;
     cudaError_t e = ok ? cudaSuccess : cudaErrorUnknown;
@@ -273,31 +282,34 @@ bool split_ready(hd_context* ctx) {
         e = cudaEventCreateWithFlags(&sp.ws_free[i], cudaEventDisableTiming);
     if (ctx->opt.record_timings)
         for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&sp.ev[i]);
-    for (int i = 0; i < 3; ++i) sp.green[i] = g[i];
-    sp.solve[0] = (cudaStream_t)st[0];
-    sp.solve[1] = (cudaStream_t)(ng == 3 ? st[2] : st[0]);
-    sp.prep = (cudaStream_t)st[1];
+    for (int i = 0; i < ng; ++i) sp.green[i] = g[i];
+    sp.prep = (cudaStream_t)st[0];
+    for (int q = 0; q < parts; ++q) sp.solve[q] = (cudaStream_t)st[1 + q];
     if (e != cudaSuccess) {
         cudaGetLastError();
         split_release(ctx);
         sp.state = -1;
         return false;
     }
-    sp.solve_sms[0] = (int)sms[0];
-    sp.solve_sms[1] = (int)sms[1];
+    for (int q = 0; q < parts; ++q) sp.solve_sms[q] = (int)sms[q];
     sp.prep_sms = (int)prep_sms;
-    sp.nws = parts == 2 ? hd_context::Split::kWorkspaces : 2;
+    sp.parts = parts;
+    sp.nws = 2 * parts;
     sp.state = 1;
     return true;
 }
 
 void split_release(hd_context* ctx) {
     hd_context::Split& sp = ctx->split;
-    for (cudaStream_t s : {sp.solve[0], sp.solve[1] != sp.solve[0] ? sp.solve[1] : nullptr, sp.prep})
+    for (cudaStream_t& s : sp.solve)
         if (s) {
             cudaStreamSynchronize(s);
             cudaStreamDestroy(s);
         }
+    if (sp.prep) {
+        cudaStreamSynchronize(sp.prep);
+        cudaStreamDestroy(sp.prep);
+    }
     for (cudaEvent_t ev : {sp.caller, sp.prep_done, sp.ev[0], sp.ev[1], sp.ev[2], sp.ev[3], sp.ev[4]})
         if (ev) cudaEventDestroy(ev);
     for (cudaEvent_t ev : sp.ws_free)
@@ -517,7 +529,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     }
     // the workspace alternates only once a dilation has been launched in it
     const int ws = split ? ctx->split.next : 0;
-    const int part = ws % 2;  // the split path's dilation partition
+    const int part = split ? ws % ctx->split.parts : 0;  // the split path's dilation partition
     DeviceArena& arena = ws ? ctx->ws_arena[ws - 1] : ctx->arena;
     cudaStream_t sq = split ? ctx->split.prep : s, sv = split ? ctx->split.solve[part] : s;
     const int prep_sms = split ? ctx->split.prep_sms : ctx->sm_count;
@@ -526,8 +538,8 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     // belong to green contexts and may still use it, so drain them first.
     auto drain_split = [&]() {
         if (ctx->split.state > 0) {
-            cudaStreamSynchronize(ctx->split.solve[0]);
-            cudaStreamSynchronize(ctx->split.solve[1]);
+            for (cudaStream_t q : ctx->split.solve)
+                if (q) cudaStreamSynchronize(q);
             cudaStreamSynchronize(ctx->split.prep);
         }
     };
@@ -545,9 +557,12 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     }
     if (total_bricks > ctx->stamp_slots || ctx->g_next > (1 << 30)) {
         const size_t want = std::max<size_t>(total_bricks, ctx->stamp_slots);
-        if (sizeof(int32_t) * want > std::min(ctx->stamps.cap, ctx->stamps2.cap)) drain_split();
+        bool grow = sizeof(int32_t) * want > ctx->stamps.cap;
+        for (const DeviceArena& a : ctx->part_stamps) grow = grow || sizeof(int32_t) * want > a.cap;
+        if (grow) drain_split();
         e = ctx->stamps.ensure(sizeof(int32_t) * want);
-        if (e == cudaSuccess) e = ctx->stamps2.ensure(sizeof(int32_t) * want);
+        for (DeviceArena& a : ctx->part_stamps)
+            if (e == cudaSuccess) e = a.ensure(sizeof(int32_t) * want);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "brick stamps");
         // the reset follows every dilation that used the stamps (split
         // path: the latest one in each workspace, which the caller's stream
@@ -557,7 +572,8 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
             e = wait_split_dilations(ctx, sq);
         }
         if (e == cudaSuccess) e = cudaMemsetAsync(ctx->stamps.ptr, 0, sizeof(int32_t) * want, sq);
-        if (e == cudaSuccess) e = cudaMemsetAsync(ctx->stamps2.ptr, 0, sizeof(int32_t) * want, sq);
+        for (DeviceArena& a : ctx->part_stamps)
+            if (e == cudaSuccess) e = cudaMemsetAsync(a.ptr, 0, sizeof(int32_t) * want, sq);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "stamp reset");
         ctx->stamp_slots = want;
         ctx->g_next = 1;
@@ -732,9 +748,9 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     sp.jobs = djobs;
     sp.states = dstates;
     for (int q = 0; q < 3; ++q) sp.queue[q] = dq[q];
-    // the split path's second dilation partition has its own stamps (its
-    // dilations may run beside those of the first)
-    sp.stamps = (int32_t*)(split && part == 1 ? ctx->stamps2.ptr : ctx->stamps.ptr);
+    // the split path's dilation partitions have stamps of their own (their
+    // dilations may run side by side)
+    sp.stamps = (int32_t*)(part > 0 ? ctx->part_stamps[part - 1].ptr : ctx->stamps.ptr);
     sp.ctl = dctl;
     sp.map[0] = ro.map_b;  // job 0 covers B
     sp.map[1] = ro.map_a;  // job 1 covers A
@@ -773,7 +789,7 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
         T.kernel = sh.kernel;
         T.steps_per_barrier = sh.steps;
         T.brick_rows = by;
-        T.dilation_partitions = ctx->split.solve[1] != ctx->split.solve[0] ? 2 : 1;
+        T.dilation_partitions = ctx->split.parts;
     }
     if (e == cudaSuccess && split) {
         e = cudaEventRecord(ctx->split.ws_free[ws], sv);
@@ -953,7 +969,7 @@ hd_status hd_context_destroy(hd_context* ctx) {
         ctx->arena.release();
         for (DeviceArena& a : ctx->ws_arena) a.release();
         ctx->stamps.release();
-        ctx->stamps2.release();
+        for (DeviceArena& a : ctx->part_stamps) a.release();
         ctx->pinned.release();
         for (int i = 0; i < hd_context::kAsyncSlots; ++i) {
             ctx->async_stage[i].release();

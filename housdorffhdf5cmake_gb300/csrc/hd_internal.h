@@ -101,9 +101,11 @@ struct hd_context {
     int g_next = 1;  // global iteration counter, monotonic across calls (brick stamps rely on it)
     hdh::DeviceArena arena;   // per-call buffers
     hdh::DeviceArena stamps;  // per-brick queue stamps, never cleared
-    // the split path's second workspace's stamps: its dilations may run
-    // beside those in the first workspace (same size and resets as stamps)
-    hdh::DeviceArena stamps2;
+    static constexpr int kMaxDilationParts = 3;  // the split path's dilation partitions, at most
+    // the stamps of the split path's dilation partitions 1, 2: their
+    // dilations may run beside those of partition 0, which uses `stamps`
+    // (same size and resets as stamps)
+    hdh::DeviceArena part_stamps[kMaxDilationParts - 1];
     size_t stamp_slots = 0;
     hdh::PinnedArena pinned;
     std::map<const void*, int> occupancy;  // persistent kernel -> resident CTAs per SM
@@ -128,18 +130,17 @@ struct hd_context {
     // the two alternate between two workspaces
     struct Split {
         int state = 0;                      // 0 not tried, 1 ready, -1 unavailable
-        // CUgreenCtx: [0] dilations in workspace 0, [1] packing and set-up,
-        // [2] dilations in workspace 1 (two dilation partitions only)
-        void* green[3] = {nullptr, nullptr, nullptr};
-        // solve[p]: the dilations of partition p (one stream for both with
-        // one dilation partition); workspace i dilates on partition i % 2
-        cudaStream_t solve[2] = {nullptr, nullptr}, prep = nullptr;
-        int solve_sms[2] = {0, 0}, prep_sms = 0;
+        // CUgreenCtx: [0] packing and set-up, [1 + p] dilation partition p
+        void* green[1 + kMaxDilationParts] = {};
+        // solve[p]: the dilations of partition p; workspace i dilates on
+        // partition i % parts
+        cudaStream_t solve[kMaxDilationParts] = {}, prep = nullptr;
+        int solve_sms[kMaxDilationParts] = {}, prep_sms = 0;
+        int parts = 1;
         cudaEvent_t caller = nullptr, prep_done = nullptr;
-        // workspaces in turn: 2 with one dilation partition, 4 with two (a
-        // pair's packing then need not wait for the dilation before last in
-        // its partition)
-        static constexpr int kWorkspaces = 4;
+        // workspaces in turn, two per dilation partition (a pair's packing
+        // then need not wait for the dilation before last in its partition)
+        static constexpr int kWorkspaces = 2 * kMaxDilationParts;
         int nws = 2;
         cudaEvent_t ws_free[kWorkspaces] = {};  // the dilation that last used workspace i
         int next = 0;

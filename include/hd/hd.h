@@ -117,7 +117,7 @@ typedef struct hd_timings {
     int32_t brick_rows;
     int32_t dilation_partitions; /* pipelined entry on split SMs: dilations in
                                     flight side by side on disjoint SM groups
-                                    (1 or 2); 0 on the other entries */
+                                    (1 to 3); 0 on the other entries */
 } hd_timings;
 
 typedef struct hd_context hd_context;

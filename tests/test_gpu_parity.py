@@ -370,11 +370,11 @@ def test_async_entry_matches_blocking_entry(hd, ctx):
                                         None) == hd.HD_ERR_BAD_ARG
 
 
-@pytest.mark.parametrize("partitions", [1, 2])
+@pytest.mark.parametrize("partitions", [1, 2, 3])
 def test_pipelined_entry_matches_blocking_entry(hd, ctx, partitions, monkeypatch):
     """hd_compute_u8_device_pipelined: back-to-back pairs (on split SMs: one
-    dilation partition with two workspaces in turn, or two side by side with
-    four; the 512x512x257 pair is above the split's size limit and runs like
+    to three dilation partitions side by side, two workspaces each in turn;
+    the 512x512x257 pair is above the split's size limit and runs like
     the asynchronous entry), a blocking call in the middle (which waits for
     the pipelined ones first), results complete after flush(), equal field by
     field to hd_compute_u8_device."""
