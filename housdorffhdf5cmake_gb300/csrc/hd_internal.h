@@ -125,9 +125,10 @@ struct hd_context {
     hdh::DeviceArena mask_stage[2];
     cudaEvent_t mask_ready[2] = {nullptr, nullptr}, mask_free[2] = {nullptr, nullptr};
     int mask_next = 0;
-    // asynchronous single pairs on split SMs (two green contexts): pair k + 1
-    // is packed and set up on a few SMs while pair k dilates on the rest;
-    // the two alternate between two workspaces
+    // asynchronous single pairs on split SMs (green contexts): pairs are
+    // packed and set up on a few SMs while earlier pairs dilate on the rest,
+    // split in up to three groups that dilate consecutive pairs side by side;
+    // the pairs take two workspaces per group in turn
     struct Split {
         int state = 0;                      // 0 not tried, 1 ready, -1 unavailable
         // CUgreenCtx: [0] packing and set-up, [1 + p] dilation partition p

@@ -181,7 +181,10 @@ hd_status hd_compute_u8_device_async(hd_context* ctx, const uint8_t* d_a, const 
  * waits for it first), so a pair's packing and set-up may run while the
  * previous pair still dilates: single pairs of up to 2^26 voxels on a GPU
  * whose SMs can be split (green contexts) run their packing and set-up on a
- * few SMs and their dilation on the rest, with two workspaces in turn.
+ * few SMs (56 on GB300) and their dilation on one of three groups of the
+ * rest (32 SMs each), consecutive pairs side by side, with two workspaces per
+ * group in turn.  A lone pair's dilation takes longer on its group than on
+ * the whole GPU: for the latency of single pairs use the other entries.
  * `stream` is made to wait for the packing's reads of the masks (not for the
  * dilation), so work queued on it after the call may overwrite or free them.
  * Otherwise the call behaves like hd_compute_u8_device_async. */
