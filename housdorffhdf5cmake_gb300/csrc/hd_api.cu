@@ -514,11 +514,12 @@ hd_status run_pairs(hd_context* ctx, const PairIn* pairs, int n, cudaStream_t s,
     const size_t pinned_bytes = upload_bytes + sizeof(hd_result) * n + (stats ? sizeof(uint64_t) * hist_words : 0);
 
     // Pipelined single pairs of up to 2^26 voxels run on split SMs: their
-    // dilation is latency-bound and fits fewer SMs, so the next pair's
-    // packing and set-up (bandwidth-bound) run beside it, on their own SMs
-    // and workspace.  Streams: sq (uploads, packing, set-up) and sv (the
-    // dilation), both the caller's stream otherwise.  The caller's stream
-    // waits for the dilations only at a flush (or the next other call).
+    // dilation is latency-bound and fits fewer SMs, so later pairs' packing
+    // and set-up run beside it, on their own SMs and workspaces, and so do
+    // consecutive pairs' dilations, on separate SM groups.  Streams: sq
+    // (uploads, packing, set-up) and sv (the dilation, on the workspace's
+    // group), both the caller's stream otherwise.  The caller's stream waits
+    // for the dilations only at a flush (or the next other call).
     const bool async = ro.async_out != nullptr;
     const bool split = async && ro.pipelined && n == 1 && sh.kernel == 2 &&
                        (double)pairs[0].W * pairs[0].H * pairs[0].D <= (double)(1 << 26) && split_ready(ctx);
