@@ -416,6 +416,40 @@ def test_pipelined_entry_matches_blocking_entry(hd, ctx, partitions, monkeypatch
     assert L.hd_pipeline_flush(None, None) == hd.HD_ERR_BAD_ARG
 
 
+def test_nonboolean_bytes(hd, ctx, oracle):
+    """Foreground = any nonzero byte (forBench/Volume.h's bool masks are one
+    byte per voxel): masks whose foreground bytes take values 1..255 in
+    every tile, and 0/1 masks with one byte per mask raised above 1 (one
+    warp of one tile then leaves the 0/1 packing path), give their 0/1
+    form's results through the device, host, batched and pipelined entries,
+    for both elements; the 0/1 form equals the oracle."""
+    rng = np.random.default_rng(29)
+    keys = ("hd", "hd_ab", "hd_ba", "sum_ab", "sum_ba", "n_a", "n_b", "n_a_not_b", "n_b_not_a", "status", "hd_robust")
+    for shape in ((33, 70, 95), (20, 48, 128)):
+        a, b = random_pair(rng, shape, p_a=0.03, p_b=0.02)
+        wide_a = (a * rng.integers(1, 256, a.shape)).astype(np.uint8)
+        wide_b = (b * rng.integers(1, 256, b.shape)).astype(np.uint8)
+        one_a, one_b = a.copy(), b.copy()
+        for m, x in ((a, one_a), (b, one_b)):
+            idx = np.flatnonzero(m)
+            x.flat[idx[len(idx) // 2]] = 0x80 + int(rng.integers(0, 128))
+        for metric in ("se6", "se18"):
+            want = ctx.compute(cuda(a), cuda(b), metric)
+            o = oracle.forbench(a, b, metric)
+            assert want["hd"] == o["hd"] and want["sum_ab"] == o["sum_ab"] and want["sum_ba"] == o["sum_ba"]
+            for va, vb in ((wide_a, wide_b), (one_a, one_b)):
+                got = [ctx.compute(cuda(va), cuda(vb), metric), ctx.compute(va, vb, metric),
+                       ctx.batch([(cuda(va), cuda(vb)), (cuda(a), cuda(b))], metric)[0]]
+                with hd.Context(0) as c:
+                    o_ = c.compute_pipelined(cuda(va), cuda(vb), metric)
+                    c.flush()
+                    torch.cuda.current_stream().synchronize()
+                    got.append(hd.result_from_bytes(o_.cpu()))
+                for g in got:
+                    for k in keys:
+                        assert g[k] == want[k], (shape, metric, k, g, want)
+
+
 def test_label_selection(hd, ctx, oracle):
     """label option (the reference's numberToLookFor): a voxel is foreground
     iff its byte equals the label; results equal the binary path on the
