@@ -831,10 +831,12 @@ hd_status hd_server_wait(hd_server* s, uint64_t ticket, int64_t timeout_ms, hd_r
     if (it == s->reqs.end()) return HD_ERR_BAD_ARG;
     Request* r = it->second.get();
     auto ready = [&] { return r->state == kDone; };
+    // one deadline for the poll and the wait that follows it
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(std::max<int64_t>(timeout_ms, 0));
     spin_wait(s, lk, ready, timeout_ms);
     if (timeout_ms < 0) {
         s->done_cv.wait(lk, ready);
-    } else if (!s->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
+    } else if (!s->done_cv.wait_until(lk, deadline, ready)) {
         return HD_ERR_NOT_READY;
     }
     *out = r->result;
@@ -845,15 +847,24 @@ hd_status hd_server_wait(hd_server* s, uint64_t ticket, int64_t timeout_ms, hd_r
 hd_status hd_server_wait_any(hd_server* s, int64_t timeout_ms, uint64_t* ticket, hd_result* out) {
     if (!s || !ticket || !out) return HD_ERR_BAD_ARG;
     std::unique_lock<std::mutex> lk(s->mu);
+    // one deadline for every round (a completion whose ticket another call
+    // took sends the loop round again)
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(std::max<int64_t>(timeout_ms, 0));
     for (;;) {
         // tickets already taken by hd_server_poll / hd_server_wait are skipped
         while (!s->done_order.empty() && !s->reqs.count(s->done_order.front())) s->done_order.pop_front();
         if (!s->done_order.empty()) break;
         auto ready = [&] { return !s->done_order.empty(); };
-        if (spin_wait(s, lk, ready, timeout_ms)) continue;
+        int64_t left_ms = -1;
+        if (timeout_ms >= 0) {
+            left_ms = std::chrono::duration_cast<std::chrono::milliseconds>(deadline - std::chrono::steady_clock::now())
+                          .count();
+            if (left_ms < 0) return HD_ERR_NOT_READY;
+        }
+        if (spin_wait(s, lk, ready, left_ms)) continue;
         if (timeout_ms < 0) {
             s->done_cv.wait(lk, ready);
-        } else if (!s->done_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) {
+        } else if (!s->done_cv.wait_until(lk, deadline, ready)) {
             return HD_ERR_NOT_READY;
         }
     }

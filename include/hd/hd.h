@@ -268,8 +268,9 @@ hd_status hd_server_create(hd_context* ctx, const hd_server_options* opt, hd_ser
 hd_status hd_server_submit(hd_server* srv, const hd_pair_desc* pair, uint64_t* ticket);
 /* HD_ERR_NOT_READY while in flight; otherwise fills *out and forgets the ticket. */
 hd_status hd_server_poll(hd_server* srv, uint64_t ticket, hd_result* out);
-/* Blocks until the request finishes (timeout_ms < 0: no limit).  The waits
- * poll (one atomic count, not the server lock) for up to 1 ms before they
+/* Blocks until the request finishes (timeout_ms < 0: no limit; else
+ * HD_ERR_NOT_READY once timeout_ms have passed).  The waits poll (one atomic
+ * count, not the server lock) for up to 1 ms (within the timeout) before they
  * sleep, and the scheduler thread polls for up to 2 ms for new requests
  * when it runs out of work: each costs a CPU core while it polls, and saves
  * a condition-variable wake-up (tens of microseconds) on a request's latency. */
