@@ -625,6 +625,10 @@ void worker_main(hd_server* s) {
     }
 }
 
+// A wait's limit in ms, from 0 up to 2^40 (35 years: the deadline in the
+// steady clock's nanoseconds cannot overflow).
+int64_t clamp_timeout_ms(int64_t timeout_ms) { return std::min<int64_t>(std::max<int64_t>(timeout_ms, 0), int64_t(1) << 40); }
+
 // Polls `ready` (server lock held by `lk`) for up to kWaitSpinUs, or
 // timeout_ms if that is shorter; true once it holds.  Between checks the
 // lock is released and only the completion count is read, without the
@@ -832,7 +836,7 @@ hd_status hd_server_wait(hd_server* s, uint64_t ticket, int64_t timeout_ms, hd_r
     Request* r = it->second.get();
     auto ready = [&] { return r->state == kDone; };
     // one deadline for the poll and the wait that follows it
-    const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(std::max<int64_t>(timeout_ms, 0));
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(clamp_timeout_ms(timeout_ms));
     spin_wait(s, lk, ready, timeout_ms);
     if (timeout_ms < 0) {
         s->done_cv.wait(lk, ready);
@@ -849,7 +853,7 @@ hd_status hd_server_wait_any(hd_server* s, int64_t timeout_ms, uint64_t* ticket,
     std::unique_lock<std::mutex> lk(s->mu);
     // one deadline for every round (a completion whose ticket another call
     // took sends the loop round again)
-    const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(std::max<int64_t>(timeout_ms, 0));
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(clamp_timeout_ms(timeout_ms));
     for (;;) {
         // tickets already taken by hd_server_poll / hd_server_wait are skipped
         while (!s->done_order.empty() && !s->reqs.count(s->done_order.front())) s->done_order.pop_front();
