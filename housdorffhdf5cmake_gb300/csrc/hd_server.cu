@@ -637,7 +637,7 @@ int64_t clamp_timeout_ms(int64_t timeout_ms) { return std::min<int64_t>(std::max
 template <class F>
 bool spin_wait(hd_server* s, std::unique_lock<std::mutex>& lk, F ready, int64_t timeout_ms) {
     const auto lim = std::chrono::microseconds(
-        timeout_ms >= 0 ? std::min<int64_t>(kWaitSpinUs, timeout_ms * 1000) : kWaitSpinUs);
+        timeout_ms >= 0 ? std::min<int64_t>(kWaitSpinUs, clamp_timeout_ms(timeout_ms) * 1000) : kWaitSpinUs);
     const auto t0 = std::chrono::steady_clock::now();
     while (!ready()) {
         const unsigned long long seen = s->done_seq.load(std::memory_order_acquire);
