@@ -8,9 +8,11 @@ The reference's own data (512x512x826 lung/bladder HDF5 masks) is not
 available; the masks are seeded synthetic stand-ins with the stated shapes.
 
   value  pairs/s with the masks resident in HBM: K pairs enqueued back to
-         back through hd_compute_u8_device_async (each result decoded on the
-         device and checked afterwards), CUDA events on the launch stream
-         around the K steps; two distinct pairs alternate so every step reads
+         back through hd_compute_u8_device_pipelined and one flush (packing
+         and set-up on a few SMs, consecutive pairs dilating side by side on
+         groups of the other SMs; each result decoded on the device and
+         checked afterwards), CUDA events on the launch stream around the K
+         steps; two distinct pairs alternate so every step reads
          masks that are not in L2 (2 x 134 MB > 126 MB L2).  The blocking
          device entry (hd_compute_u8_device) is reported beside it
   e2e    pairs/s with pinned HOST masks through hd_compute_u8_async: each
