@@ -168,7 +168,8 @@ def bench_ours(args):
         blocking.append(e0.elapsed_time(e1))
     phases = phases[-2:]
     # warm-up of the enqueue-only entries used in the timed regions (the
-    # first pipelined call sets up the split SMs and the second workspace)
+    # first pipelined calls set up the split SMs and allocate the six
+    # workspaces, one per call)
     outs = torch.empty((args.steps, hd.RESULT_BYTES), dtype=torch.uint8, device=dev)
     for w in range(max(args.warmup, 6)):
         x, y = pairs[w % 2]
@@ -180,8 +181,8 @@ def bench_ours(args):
     # ---- device-resident timed region ---------------------------------------
     # K pairs enqueued back to back through hd_compute_u8_device_pipelined
     # (each result decoded on the device into its own slot; a pair's packing
-    # and set-up run beside the previous pair's dilation), one flush, one
-    # synchronisation
+    # and set-up run beside earlier pairs' dilations, which run side by side
+    # on groups of SMs), one flush, one synchronisation
     clocks = ClockSampler(local)
     with clocks:
         if dist:
